@@ -1,0 +1,480 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 hierarchical RMQ path.
+
+Workload (N = 1): the plain single-array configuration — n = 2^26 fp32 values
+uniform in [0, 1), q = 2^26 inclusive queries with lengths
+clamp(round(exp(N(ln 2^13, 1))), 1, n) and l uniform in [0, n - len]; every
+query returns its fp32 minimum and its int32 argmin (ties to the lowest
+index).  One step is one pass of the query kernel over all q queries with the
+array, the hierarchy and the queries resident in HBM.  The inputs (1 GiB of
+queries and values, 512 MiB of outputs) exceed the 129 MB L2, so no flush is
+needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun each rank builds and queries its own replica on its own GPU
+(no collective on the data path); value = all ranks' queries / max-over-ranks
+time ("weak" scaling).  The reference arm (--impl reference) times the
+reference's CPU brute-force scan (restated in oracle/) on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+PKG = ROOT / "gpu-rmq_gb300"
+for _p in (str(ROOT), str(PKG)):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "RMQ queries/s"
+UNIT = "queries/s"
+CANON_RF_LOG = 5   # canonical descent for algorithmic bytes: rf_c = 32 (128-B lines)
+SECTOR = 32
+
+
+# ---------------------------------------------------------------------------
+# Algorithmic bytes (implementation independent): per query, 8 B of query,
+# 4 B of min, 4 B of argmin, plus the 32-B sectors of the input array that
+# the canonical descent (rf = 32) reads at level 0: the sectors of [l, r] when
+# len <= 64, else those of [l, ceil32(l)) and [floor32(r+1), r+1).
+# ---------------------------------------------------------------------------
+def level0_sectors(qs: np.ndarray, n: int) -> np.ndarray:
+    l = qs[:, 0].astype(np.int64)
+    r = qs[:, 1].astype(np.int64)
+    e = r + 1
+    rf = 1 << CANON_RF_LOG
+    short = (e - l) <= 2 * rf
+    if n <= 64:
+        short[:] = True
+    s_short = (r >> 3) - (l >> 3) + 1
+    nl = (l + rf - 1) & ~(rf - 1)
+    pr = e & ~(rf - 1)
+    left = np.where(nl > l, ((nl - 1) >> 3) - (l >> 3) + 1, 0)
+    right = np.where(e > pr, (r >> 3) - (pr >> 3) + 1, 0)
+    return np.where(short, s_short, left + right)
+
+
+def algorithmic_bytes(qs: np.ndarray, n: int, with_min: bool, with_idx: bool) -> int:
+    per_q = 8 + (4 if with_min else 0) + (4 if with_idx else 0)
+    return int(per_q * qs.shape[0] + SECTOR * int(level0_sectors(qs, n).sum()))
+
+
+def measured_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def traffic_per_query(kernel_tag: str) -> float | None:
+    """DRAM bytes per query of the query kernel from the committed ncu summary
+    (a line `traffic_bytes_per_query[<tag>]: X`), or None."""
+    for p in sorted((ROOT / "profiles").glob("*.md")):
+        for line in p.read_text().splitlines():
+            key = f"traffic_bytes_per_query[{kernel_tag}]:"
+            if line.strip().startswith(key):
+                try:
+                    return float(line.split(":", 1)[1].strip().split()[0])
+                except ValueError:
+                    return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active," \
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown," \
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+        self.thread = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+            time.sleep(0.25)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            time.sleep(0.15)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            if self.thread:
+                self.thread.join(timeout=2)
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": mx, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# distributed helpers (one process per GPU; timing reduction only)
+# ---------------------------------------------------------------------------
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def dist_init(ws: int, backend: str):
+    if ws <= 1:
+        return None
+    import torch.distributed as dist
+    if not dist.is_initialized():
+        dist.init_process_group(backend=backend)
+    return dist
+
+
+def max_over_ranks(x: float, ws: int, device=None) -> float:
+    if ws <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(ws: int):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+# ---------------------------------------------------------------------------
+def make_inputs(n: int, q: int, lr: int, seed: int):
+    import rmq_gb300 as R
+    a = R.gen_array(n, seed)
+    qs = R.gen_queries(q, lr, n, seed)
+    return a, qs
+
+
+def cpu_baseline(a: np.ndarray, qs: np.ndarray, budget_s: float, with_idx: bool = True) -> dict:
+    """The reference's brute-force scan (oracle/ restatement of cpu_rmq /
+    cpu_rmq_idx) on all host threads over consecutive chunks of the same
+    query set until `budget_s` of wall time is used."""
+    from oracle import oracle
+    threads = oracle.max_threads()
+    chunk = 1 << 14
+    done = 0
+    t0 = time.perf_counter()
+    while done < qs.shape[0] and time.perf_counter() - t0 < budget_s:
+        part = qs[done: done + chunk]
+        oracle.rmq_min(a, part, threads)
+        if with_idx:
+            oracle.rmq_argmin(a, part, threads)
+        done += part.shape[0]
+    dt = time.perf_counter() - t0
+    return {"value": done / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"first {done} of the {qs.shape[0]} queries (min{' + argmin' if with_idx else ''}), "
+                      f"{dt:.1f} s wall on {threads} threads"}
+
+
+def run_reference(args, ws, rank):
+    """Reference arm: the reference's CPU scan (alg 0 + alg 100 semantics) on
+    the host cores, rank 0 only; each step is a bounded sample."""
+    if rank != 0:
+        return
+    from oracle import oracle
+    a, qs = make_inputs(args.n, args.q, args.lr, args.seed)
+    threads = oracle.max_threads()
+    per_step = args.ref_step_queries
+    rng = np.random.default_rng(args.seed)
+    times = []
+    for i in range(args.warmup + args.steps):
+        start = int(rng.integers(0, max(1, qs.shape[0] - per_step)))
+        part = qs[start: start + per_step]
+        t0 = time.perf_counter()
+        oracle.rmq_min(a, part, threads)
+        oracle.rmq_argmin(a, part, threads)
+        dt = time.perf_counter() - t0
+        if i >= args.warmup:
+            times.append(dt)
+    ms = 1e3 * statistics.mean(times)
+    value = per_step / (ms / 1e3)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": workload_config(args),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{per_step} consecutive queries per step (random offset), "
+                                   f"min + argmin brute-force scan on {threads} threads"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def workload_config(args) -> dict:
+    return {"workload": f"plain single array: n=2^{int(np.log2(args.n))} fp32 uniform[0,1), "
+                        f"q=2^{int(np.log2(args.q))} queries, len=clamp(round(exp(N(ln 2^13,1))),1,n), "
+                        f"l uniform in [0,n-len]; min + argmin per query",
+            "n": args.n, "q": args.q, "lr_code": args.lr, "seed": args.seed,
+            "variant": args.variant, "scan_threshold": args.t, "rf_log": args.rf_log, "lanes": args.lanes,
+            "l2": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{dist_env()[0]}"}
+
+
+def run_ours(args, ws, rank, local):
+    import torch
+    import rmq_gb300 as R
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    dist_init(ws, "nccl")
+
+    a, qs = make_inputs(args.n, args.q, args.lr, args.seed + rank)
+    q = qs.shape[0]
+    dv = torch.from_numpy(a).to(dev)
+    dq = torch.from_numpy(qs.view(np.int32)).to(dev)
+    out_min = torch.empty(q, dtype=torch.float32, device=dev)
+    out_idx = torch.empty(q, dtype=torch.int32, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    sh = stream.cuda_stream
+
+    h = R.Hierarchy(dv, variant=args.variant, t=args.t, rf_log=args.rf_log, lanes=args.lanes,
+                    l2_persist=args.l2_persist, stream=stream)
+    info = h.info()
+    torch.cuda.synchronize()
+
+    lr_ptr, idx_ptr, min_ptr = int(dq.data_ptr()), int(out_idx.data_ptr()), int(out_min.data_ptr())
+
+    def step():
+        st = h.query_idx_raw(lr_ptr, q, idx_ptr, min_ptr, sh)
+        if st != 0:
+            raise R.RMQError(st, "rmq_query_idx")
+
+    # --- device-resident throughput -------------------------------------------
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            step()
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    barrier(ws)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        with torch.cuda.stream(stream):
+            ev[0].record(stream)
+            for k in range(args.steps):
+                step()
+                ev[k + 1].record(stream)
+        torch.cuda.synchronize()
+    barrier(ws)
+    per_launch = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
+    total_ms = ev[0].elapsed_time(ev[args.steps])
+    total_ms = max_over_ranks(total_ms, ws, dev)
+    ms_step = total_ms / args.steps
+    value = ws * q * args.steps / (total_ms / 1e3)
+
+    # --- minimum-only pass (same kernel family, no argmin), for reference ------
+    with torch.cuda.stream(stream):
+        for _ in range(max(1, args.warmup)):
+            h.query_raw(lr_ptr, q, min_ptr, sh)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            h.query_raw(lr_ptr, q, min_ptr, sh)
+        e1.record(stream)
+    torch.cuda.synchronize()
+    min_only_qps = q * args.steps / (e0.elapsed_time(e1) / 1e3)
+
+    # --- end to end: pinned host queries -> device -> host results -------------
+    e2e = run_e2e(args, h, qs, dev, ws)
+
+    # --- parity spot check of the timed outputs (not timed) ---------------------
+    from oracle import oracle
+    samp = R.sample_indices(q, 1 << 12, args.seed).astype(np.int64)
+    got_m = out_min.cpu().numpy()[samp]
+    got_i = out_idx.cpu().numpy().view(np.uint32)[samp]
+    exp_m = oracle.rmq_min(a, qs[samp])
+    exp_i = oracle.rmq_argmin(a, qs[samp])
+    parity = bool(got_m.tobytes() == exp_m.tobytes() and np.array_equal(got_i, exp_i))
+
+    peaks = measured_peaks()
+    alg_bytes = algorithmic_bytes(qs, args.n, True, True)
+    kernel_ms = statistics.mean(per_launch)
+    achieved = alg_bytes / (kernel_ms / 1e3) / 1e9
+    tpq = traffic_per_query(f"{info.variant}-rf{1 << info.rf_log}")
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved / peaks["hbm_gbs"],
+                "traffic": (tpq * q) if tpq is not None else None,
+                "peak_source": f"{peaks['source']} (MEASURED_PEAKS.json hbm_gbs, copy burst)",
+                "algorithmic_bytes_per_launch": alg_bytes,
+                "kernel": "query_%s_kernel (argmin+min)" % ("vl" if info.variant == 2 else "cl"),
+                "kernel_ms_mean": kernel_ms}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(a, qs, args.cpu_budget)
+
+    build_bytes = 4 * args.n + 8 * sum(info.sizes()[1:])
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generators; no public dataset)",
+        "config": workload_config(args),
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "clocks": clocks.summary(),
+        "gpu_launches": args.steps,
+        "parity_sample_ok": parity,
+        "min_only_queries_per_s": min_only_qps,
+        "hierarchy": {"variant": ["auto", "cl", "vl"][info.variant], "rf": 1 << info.rf_log,
+                      "t": int(info.scan_threshold), "levels": int(info.num_levels),
+                      "lanes": int(info.lanes), "level_bytes": int(info.level_bytes),
+                      "build_ms": float(info.build_ms),
+                      "build_GBps": build_bytes / (float(info.build_ms) / 1e3) / 1e9 if info.build_ms > 0 else None},
+    }
+    h.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def run_e2e(args, h, qs, dev, ws) -> dict:
+    """Same metric through the C ABI with host buffers: every step copies the
+    queries from pinned host memory, answers them and copies min + argmin back,
+    in chunks pipelined over two streams (copy of chunk i+1 overlaps the
+    kernel of chunk i and the copy back of chunk i-1)."""
+    import torch
+    q = qs.shape[0]
+    chunk = min(q, args.e2e_chunk)
+    nchunks = (q + chunk - 1) // chunk
+    h_q = torch.from_numpy(qs.view(np.int32).reshape(-1)).pin_memory()
+    h_min = torch.empty(q, dtype=torch.float32).pin_memory()
+    h_idx = torch.empty(q, dtype=torch.int32).pin_memory()
+    nbuf = 3
+    d_q = [torch.empty(2 * chunk, dtype=torch.int32, device=dev) for _ in range(nbuf)]
+    d_min = [torch.empty(chunk, dtype=torch.float32, device=dev) for _ in range(nbuf)]
+    d_idx = [torch.empty(chunk, dtype=torch.int32, device=dev) for _ in range(nbuf)]
+    s_h2d = torch.cuda.Stream(device=dev)
+    s_cmp = torch.cuda.Stream(device=dev)
+    s_d2h = torch.cuda.Stream(device=dev)
+    launches = [0]
+
+    def one_pass():
+        done_h2d = [torch.cuda.Event() for _ in range(nchunks)]
+        done_cmp = [torch.cuda.Event() for _ in range(nchunks)]
+        done_d2h = [None] * nbuf
+        for c in range(nchunks):
+            b = c % nbuf
+            lo = c * chunk
+            m = min(chunk, q - lo)
+            with torch.cuda.stream(s_h2d):
+                if done_d2h[b] is not None:
+                    s_h2d.wait_event(done_d2h[b])
+                d_q[b][: 2 * m].copy_(h_q[2 * lo: 2 * (lo + m)], non_blocking=True)
+                done_h2d[c].record(s_h2d)
+            with torch.cuda.stream(s_cmp):
+                s_cmp.wait_event(done_h2d[c])
+                st = h.query_idx_raw(int(d_q[b].data_ptr()), m, int(d_idx[b].data_ptr()),
+                                     int(d_min[b].data_ptr()), s_cmp.cuda_stream)
+                if st != 0:
+                    raise RuntimeError(f"rmq_query_idx failed: {st}")
+                launches[0] += 1
+                done_cmp[c].record(s_cmp)
+            with torch.cuda.stream(s_d2h):
+                s_d2h.wait_event(done_cmp[c])
+                h_min[lo: lo + m].copy_(d_min[b][:m], non_blocking=True)
+                h_idx[lo: lo + m].copy_(d_idx[b][:m], non_blocking=True)
+                ev = torch.cuda.Event()
+                ev.record(s_d2h)
+                done_d2h[b] = ev
+
+    for _ in range(args.warmup):
+        one_pass()
+    torch.cuda.synchronize()
+    barrier(ws)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        one_pass()
+    torch.cuda.synchronize()
+    dt = max_over_ranks(time.perf_counter() - t0, ws, dev)
+    return {"value": ws * q * args.steps / dt, "unit": UNIT, "h2d_bytes_per_step": 8 * q,
+            "d2h_bytes_per_step": 8 * q, "chunk_queries": chunk, "kernel_launches_per_step": nchunks}
+
+
+def parse_args(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n", type=int, default=1 << 26)
+    ap.add_argument("--q", type=int, default=1 << 26)
+    ap.add_argument("--lr", type=int, default=-7, help="length law code (-7 = lognormal median 2^13 sigma 1)")
+    ap.add_argument("--seed", type=int, default=42)
+    ap.add_argument("--variant", default="auto", choices=["auto", "cl", "vl"])
+    ap.add_argument("--t", type=int, default=1 << 10, help="scan threshold")
+    ap.add_argument("--rf-log", dest="rf_log", type=int, default=0)
+    ap.add_argument("--lanes", type=int, default=0)
+    ap.add_argument("--l2-persist", dest="l2_persist", action="store_true")
+    ap.add_argument("--e2e-chunk", dest="e2e_chunk", type=int, default=1 << 22)
+    ap.add_argument("--cpu-budget", dest="cpu_budget", type=float, default=10.0)
+    ap.add_argument("--no-cpu-baseline", dest="no_cpu_baseline", action="store_true")
+    ap.add_argument("--ref-step-queries", dest="ref_step_queries", type=int, default=1 << 14)
+    args = ap.parse_args(argv)
+    args.warmup = max(3, args.warmup)  # timing rule: at least 3 untimed warm-up steps
+    return args
+
+
+def main(argv=None):
+    args = parse_args(argv)
+    ws, rank, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+        return
+    run_ours(args, ws, rank, local)
+
+
+if __name__ == "__main__":
+    main()

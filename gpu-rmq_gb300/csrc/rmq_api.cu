@@ -1,0 +1,316 @@
+// rmq_api.cu — implementation of the C ABI declared in include/rmq_gb300.h.
+//
+// Replaces the host drivers xxx_rmq (src/xxx.h:203-298) and
+// hierarchical_vector_load (src/xxx.h:932-1040): those validate t, lay out the
+// levels, allocate, build, time `reps` query launches with a device-wide sync
+// after each, and return a host array.  Here the build and the queries are
+// separate, stream-ordered calls; the handle owns the level buffers, the caller
+// owns inputs and outputs, and every failure is a status code (the reference
+// exits the process on a bad t, src/xxx.h:211-217).
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+
+#include "../../include/rmq_gb300.h"
+#include "rmq_internal.h"
+
+using rmq::Layout;
+
+struct rmq_handle {
+    Layout lay;
+    const float* d_values = nullptr;
+    float* val_buf = nullptr;
+    uint32_t* idx_buf = nullptr;
+    uint32_t* err = nullptr;  // invalid-query counter (validate mode)
+    int device = 0;
+    int variant = RMQ_VARIANT_VL;
+    int lanes = 8;
+    int with_index = 1;
+    int l2_persist = 0;
+    int validate = 0;
+    size_t persist_bytes = 0;
+    float build_ms = 0.f;
+    std::mutex validate_mu;
+};
+
+namespace {
+
+// Variant defaults: the paper's chosen configurations (CL: 16 lanes x 2
+// entries, rf = 32, t = 64; VL: rf = 8, t = 32), as selected by
+// scripts/get_and_filter_data.py:11 and scripts/static_data.py:251-253.
+constexpr int kClRfLog = 5;
+constexpr uint64_t kClT = 64;
+constexpr int kClLanes = 8;
+constexpr int kVlRfLog = 3;
+constexpr uint64_t kVlT = 32;
+
+// Largest supported n: queries are uint32 pairs and the descent rounds r up by
+// at most rf - 1 without overflowing 32 bits.
+constexpr uint64_t kMaxN = 0xFFFFFF00ull;
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+        if (cudaGetDevice(&prev) == cudaSuccess && prev != dev) cudaSetDevice(dev);
+        else prev = -1;
+    }
+    ~DeviceGuard() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
+
+int cuda_status(cudaError_t e) {
+    if (e == cudaSuccess) return RMQ_OK;
+    if (e == cudaErrorMemoryAllocation) return RMQ_ERR_OOM;
+    return RMQ_ERR_CUDA;
+}
+
+int resolve_config(uint64_t n, const rmq_config* cfg_in, int* variant, int* rf_log,
+                   uint64_t* t, int* lanes) {
+    rmq_config cfg;
+    if (cfg_in != nullptr) cfg = *cfg_in;
+    else rmq_config_init(&cfg);
+    int v = cfg.variant;
+    if (v == RMQ_VARIANT_AUTO) v = RMQ_VARIANT_VL;
+    if (v != RMQ_VARIANT_CL && v != RMQ_VARIANT_VL) return RMQ_ERR_ARG;
+    int r = cfg.rf_log != 0 ? cfg.rf_log : (v == RMQ_VARIANT_CL ? kClRfLog : kVlRfLog);
+    if (r < 3 || r > 5) return RMQ_ERR_ARG;
+    uint64_t tt = cfg.scan_threshold != 0 ? cfg.scan_threshold : (v == RMQ_VARIANT_CL ? kClT : kVlT);
+    const uint64_t rf = uint64_t(1) << r;
+    // The reference's own preconditions (src/xxx.h:211, src/xxx.h:938).
+    if (v == RMQ_VARIANT_CL && tt < 2 * rf) return RMQ_ERR_ARG;
+    if (v == RMQ_VARIANT_VL && tt < rf) return RMQ_ERR_ARG;
+    int g = cfg.lanes != 0 ? cfg.lanes : kClLanes;
+    if (g != 4 && g != 8 && g != 16 && g != 32) return RMQ_ERR_ARG;
+    (void)n;
+    *variant = v;
+    *rf_log = r;
+    *t = tt;
+    *lanes = g;
+    return RMQ_OK;
+}
+
+void fill_info(const Layout& lay, int variant, int lanes, rmq_info* info) {
+    std::memset(info, 0, sizeof(*info));
+    info->num_levels = lay.num_levels;
+    info->rf_log = lay.rf_log;
+    info->variant = variant;
+    info->lanes = lanes;
+    info->n = lay.n;
+    info->scan_threshold = lay.t;
+    for (uint32_t k = 0; k < lay.num_levels && k < 20; ++k) {
+        info->level_size[k] = lay.size[k];
+        info->level_offset[k] = k == 0 ? ~uint64_t(0) : lay.offset[k];
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+void rmq_config_init(rmq_config* cfg) {
+    if (cfg == nullptr) return;
+    std::memset(cfg, 0, sizeof(*cfg));
+    cfg->variant = RMQ_VARIANT_AUTO;
+    cfg->with_index = 1;
+}
+
+const char* rmq_strerror(int status) {
+    switch (status) {
+        case RMQ_OK: return "ok";
+        case RMQ_ERR_ARG: return "invalid argument";
+        case RMQ_ERR_CUDA: return "CUDA runtime error";
+        case RMQ_ERR_OOM: return "device out of memory";
+        case RMQ_ERR_QUERY_RANGE: return "query out of range (l > r or r >= n)";
+        case RMQ_ERR_TIMEOUT: return "device-side wait timed out";
+        case RMQ_ERR_NO_INDEX: return "handle was built without argmin arrays";
+        case RMQ_ERR_UNSUPPORTED: return "unsupported size or configuration";
+        default: return "unknown status";
+    }
+}
+
+int rmq_plan_layout(uint64_t n, uint64_t scan_threshold, int32_t rf_log, int32_t variant,
+                    rmq_info* info) {
+    if (info == nullptr || n == 0) return RMQ_ERR_ARG;
+    if (n > kMaxN) return RMQ_ERR_UNSUPPORTED;
+    rmq_config cfg;
+    rmq_config_init(&cfg);
+    cfg.variant = variant;
+    cfg.scan_threshold = scan_threshold;
+    cfg.rf_log = rf_log;
+    int v, r, g;
+    uint64_t t;
+    const int st = resolve_config(n, &cfg, &v, &r, &t, &g);
+    if (st != RMQ_OK) return st;
+    const Layout lay = rmq::plan_layout(n, t, uint32_t(r));
+    fill_info(lay, v, g, info);
+    return RMQ_OK;
+}
+
+int rmq_build(const float* d_values, uint64_t n, const rmq_config* cfg, rmq_stream_t stream,
+              rmq_handle** out) {
+    if (out == nullptr) return RMQ_ERR_ARG;
+    *out = nullptr;
+    if (d_values == nullptr || n == 0) return RMQ_ERR_ARG;
+    if ((reinterpret_cast<uintptr_t>(d_values) & 31u) != 0) return RMQ_ERR_ARG;
+    if (n > kMaxN) return RMQ_ERR_UNSUPPORTED;
+    int v, r, g;
+    uint64_t t;
+    int st = resolve_config(n, cfg, &v, &r, &t, &g);
+    if (st != RMQ_OK) return st;
+
+    rmq_handle* h = new (std::nothrow) rmq_handle();
+    if (h == nullptr) return RMQ_ERR_OOM;
+    if (cudaGetDevice(&h->device) != cudaSuccess) {
+        delete h;
+        return RMQ_ERR_CUDA;
+    }
+    h->lay = rmq::plan_layout(n, t, uint32_t(r));
+    h->d_values = d_values;
+    h->variant = v;
+    h->lanes = g;
+    h->with_index = cfg != nullptr ? (cfg->with_index != 0) : 1;
+    h->l2_persist = cfg != nullptr ? cfg->l2_persist : 0;
+    h->validate = cfg != nullptr ? cfg->validate : 0;
+
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    cudaError_t e = cudaSuccess;
+    if (h->lay.num_levels > 1) {
+        e = cudaMalloc(&h->val_buf, h->lay.total * sizeof(float));
+        if (e == cudaSuccess && h->with_index) e = cudaMalloc(&h->idx_buf, h->lay.total * sizeof(uint32_t));
+    }
+    if (e == cudaSuccess) e = cudaMalloc(&h->err, sizeof(uint32_t));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        rmq_destroy(h);
+        return cuda_status(e);
+    }
+
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    if (e == cudaSuccess) e = cudaEventRecord(e0, s);
+    if (e == cudaSuccess) e = rmq::launch_build(h->lay, d_values, h->val_buf, h->idx_buf, s);
+    if (e == cudaSuccess) e = cudaEventRecord(e1, s);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&h->build_ms, e0, e1);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        rmq_destroy(h);
+        return cuda_status(e);
+    }
+
+    if (h->l2_persist && h->lay.num_levels > 1) {
+        int max_persist = 0, max_window = 0;
+        cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, h->device);
+        cudaDeviceGetAttribute(&max_window, cudaDevAttrMaxAccessPolicyWindowSize, h->device);
+        size_t bytes = h->lay.total * sizeof(float);
+        if (bytes > size_t(max_window)) bytes = size_t(max_window);
+        if (bytes > size_t(max_persist)) bytes = size_t(max_persist);
+        if (bytes > 0) {
+            size_t cur = 0;
+            cudaDeviceGetLimit(&cur, cudaLimitPersistingL2CacheSize);
+            if (cur < bytes) cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, bytes);
+            h->persist_bytes = bytes;
+        }
+        cudaGetLastError();
+    }
+    *out = h;
+    return RMQ_OK;
+}
+
+static int query_common(const rmq_handle* hc, const uint32_t* d_lr, uint64_t q, float* d_min,
+                        uint32_t* d_argmin, rmq_stream_t stream) {
+    if (hc == nullptr) return RMQ_ERR_ARG;
+    if (q == 0) return RMQ_OK;
+    if (q > 0xFFFFFFFFull) return RMQ_ERR_UNSUPPORTED;
+    if (d_lr == nullptr || (reinterpret_cast<uintptr_t>(d_lr) & 7u) != 0) return RMQ_ERR_ARG;
+    if (d_min == nullptr && d_argmin == nullptr) return RMQ_ERR_ARG;
+    if (d_argmin != nullptr && !hc->with_index && hc->lay.num_levels > 1) return RMQ_ERR_NO_INDEX;
+    rmq_handle* h = const_cast<rmq_handle*>(hc);
+    DeviceGuard guard(h->device);
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+
+    rmq::QueryArgs a;
+    std::memset(&a, 0, sizeof(a));
+    for (uint32_t k = 0; k < h->lay.num_levels; ++k) {
+        a.lv.val[k] = k == 0 ? h->d_values : h->val_buf + h->lay.offset[k];
+        a.lv.idx[k] = (k == 0 || h->idx_buf == nullptr) ? nullptr : h->idx_buf + h->lay.offset[k];
+        a.lv.size[k] = uint32_t(h->lay.size[k]);
+    }
+    a.lv.num_levels = h->lay.num_levels;
+    a.qs = reinterpret_cast<const uint2*>(d_lr);
+    a.q = uint32_t(q);
+    a.out_min = d_min;
+    a.out_idx = d_argmin;
+    a.variant = h->variant;
+    a.lanes = h->lanes;
+    a.rf_log = h->lay.rf_log;
+    a.persist_base = h->persist_bytes ? h->val_buf : nullptr;
+    a.persist_bytes = h->persist_bytes;
+
+    if (!h->validate) {
+        a.err = nullptr;
+        return cuda_status(rmq::launch_query(a, s));
+    }
+    std::lock_guard<std::mutex> lock(h->validate_mu);
+    a.err = h->err;
+    cudaError_t e = cudaMemsetAsync(h->err, 0, sizeof(uint32_t), s);
+    if (e == cudaSuccess) e = rmq::launch_query(a, s);
+    uint32_t bad = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&bad, h->err, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_status(e);
+    return bad ? RMQ_ERR_QUERY_RANGE : RMQ_OK;
+}
+
+int rmq_query(const rmq_handle* h, const uint32_t* d_lr, uint64_t q, float* d_min,
+              rmq_stream_t stream) {
+    if (d_min == nullptr) return RMQ_ERR_ARG;
+    return query_common(h, d_lr, q, d_min, nullptr, stream);
+}
+
+int rmq_query_idx(const rmq_handle* h, const uint32_t* d_lr, uint64_t q, uint32_t* d_argmin,
+                  float* d_min_or_null, rmq_stream_t stream) {
+    if (d_argmin == nullptr) return RMQ_ERR_ARG;
+    return query_common(h, d_lr, q, d_min_or_null, d_argmin, stream);
+}
+
+int rmq_scan_bruteforce(const float* d_values, uint64_t n, const uint32_t* d_lr, uint64_t q,
+                        float* d_min_or_null, uint32_t* d_argmin_or_null, rmq_stream_t stream) {
+    if (q == 0) return RMQ_OK;
+    if (d_values == nullptr || n == 0 || d_lr == nullptr) return RMQ_ERR_ARG;
+    if (d_min_or_null == nullptr && d_argmin_or_null == nullptr) return RMQ_ERR_ARG;
+    if (n > kMaxN || q > 0xFFFFFFFFull) return RMQ_ERR_UNSUPPORTED;
+    if ((reinterpret_cast<uintptr_t>(d_lr) & 7u) != 0) return RMQ_ERR_ARG;
+    return cuda_status(rmq::launch_bruteforce(d_values, uint32_t(n), reinterpret_cast<const uint2*>(d_lr),
+                                              uint32_t(q), d_min_or_null, d_argmin_or_null,
+                                              reinterpret_cast<cudaStream_t>(stream)));
+}
+
+int rmq_get_info(const rmq_handle* h, rmq_info* info) {
+    if (h == nullptr || info == nullptr) return RMQ_ERR_ARG;
+    fill_info(h->lay, h->variant, h->lanes, info);
+    info->level_bytes = h->lay.num_levels > 1
+                            ? h->lay.total * (sizeof(float) + (h->idx_buf ? sizeof(uint32_t) : 0))
+                            : 0;
+    info->build_ms = h->build_ms;
+    return RMQ_OK;
+}
+
+void rmq_destroy(rmq_handle* h) {
+    if (h == nullptr) return;
+    {
+        DeviceGuard guard(h->device);
+        if (h->val_buf) cudaFree(h->val_buf);
+        if (h->idx_buf) cudaFree(h->idx_buf);
+        if (h->err) cudaFree(h->err);
+        cudaGetLastError();
+    }
+    delete h;
+}
+
+}  // extern "C"

@@ -1,0 +1,136 @@
+// rmq_common.cuh — layout and device helpers shared by the build and query kernels.
+//
+// The structure is the reference's multi-level block-minimum hierarchy
+// (metadata struct src/constants.cuh:34-39, layout loop src/xxx.h:225-243):
+// level 0 is the caller's array; level k+1 holds, for every aligned chunk of
+// rf = 2^R entries of level k, the chunk minimum.  This build also stores,
+// next to every block minimum, the level-0 index of its first occurrence so
+// that argmin queries need one extra load instead of a second descent.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace rmq {
+
+constexpr int kMaxLevels = 20;            // XXX_MAX_LEVELS, src/constants.cuh:14
+constexpr uint32_t kLevelAlign = 32;      // XXX_LEVEL_ALIGNMENT, src/constants.cuh:15 (entries)
+constexpr uint32_t kNoPos = 0xFFFFFFFFu;  // "no candidate" / invalid-query argmin
+
+// Host-side description of the hierarchy (sizes in entries).
+struct Layout {
+    uint32_t num_levels = 1;
+    uint32_t rf_log = 3;
+    uint64_t n = 0;
+    uint64_t t = 0;
+    uint64_t size[kMaxLevels] = {};
+    uint64_t offset[kMaxLevels] = {};  // offset of level k >= 1 inside the level buffer
+    uint64_t total = 0;                // entries in the level buffer incl. alignment padding
+};
+
+// Device-side view passed by value to the kernels (fits easily in the 32 KB
+// parameter space).
+struct Levels {
+    const float* val[kMaxLevels];      // val[0] = caller's array
+    const uint32_t* idx[kMaxLevels];   // idx[k] (k >= 1): level-0 index of block k's first minimum
+    uint32_t size[kMaxLevels];
+    uint32_t num_levels;
+};
+
+// ---------------------------------------------------------------------------
+// Memory access helpers (inline PTX; sm_100+ 256-bit global loads).  The
+// loads read data that no kernel writes while queries run, so they are not
+// volatile: the compiler may batch independent loads before their first use.
+// ---------------------------------------------------------------------------
+
+// 32-byte (one sector) load through the non-coherent path; the caller
+// guarantees 32-byte alignment and that all 8 floats lie inside the buffer.
+__device__ __forceinline__ void ld_sector(const float* p, float (&v)[8]) {
+    asm(
+        "ld.global.nc.L1::no_allocate.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]),
+          "=f"(v[4]), "=f"(v[5]), "=f"(v[6]), "=f"(v[7])
+        : "l"(p));
+}
+
+// Same load with an explicit L2 cache policy (createpolicy result).
+__device__ __forceinline__ void ld_sector_policy(const float* p, float (&v)[8], uint64_t pol) {
+    asm(
+        "ld.global.nc.L1::no_allocate.L2::cache_hint.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8], %9;"
+        : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]),
+          "=f"(v[4]), "=f"(v[5]), "=f"(v[6]), "=f"(v[7])
+        : "l"(p), "l"(pol));
+}
+
+__device__ __forceinline__ void ld_quad(const float* p, float (&v)[4]) {
+    asm("ld.global.nc.L1::no_allocate.v4.f32 {%0,%1,%2,%3}, [%4];"
+                 : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3])
+                 : "l"(p));
+}
+
+__device__ __forceinline__ uint64_t policy_evict_last() {
+    uint64_t pol;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+
+__device__ __forceinline__ uint64_t policy_evict_first() {
+    uint64_t pol;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+
+// Streaming query load of one {l, r} pair; the query array is read once, so
+// it is marked evict-first in L2 to leave room for the coarse levels.
+__device__ __forceinline__ uint2 ld_query(const uint2* p) {
+    uint2 v;
+    asm(
+        "{\n\t.reg .b64 pol;\n\t"
+        "createpolicy.fractional.L2::evict_first.b64 pol, 1.0;\n\t"
+        "ld.global.nc.L1::no_allocate.L2::cache_hint.v2.u32 {%0,%1}, [%2], pol;\n\t}"
+        : "=r"(v.x), "=r"(v.y) : "l"(p));
+    return v;
+}
+
+__device__ __forceinline__ void st_stream(float* p, float v) {
+    asm volatile("st.global.cs.f32 [%0], %1;" :: "l"(p), "f"(v) : "memory");
+}
+__device__ __forceinline__ void st_stream(uint32_t* p, uint32_t v) {
+    asm volatile("st.global.cs.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
+}
+
+// ---------------------------------------------------------------------------
+// Candidate ordering.  A candidate is an entry of some level together with the
+// level-0 position of its block start.  The pieces a query visits partition
+// [l, r], so positions are unique and ordering candidates by (value, position)
+// with IEEE "<" on the value reproduces the brute-force scan's
+// "first occurrence of the minimum" (src/cpu_methods.h:42-53).
+// ---------------------------------------------------------------------------
+struct Cand {
+    float v;
+    uint32_t pos;   // level-0 position of the candidate's block start
+    uint32_t lvl;   // level the candidate came from
+};
+
+__device__ __forceinline__ void cand_init(Cand& c) {
+    c.v = __int_as_float(0x7f800000);  // +inf
+    c.pos = kNoPos;
+    c.lvl = 0;
+}
+
+__device__ __forceinline__ bool cand_better(float v, uint32_t pos, const Cand& c) {
+    return (v < c.v) | ((v == c.v) & (pos < c.pos));
+}
+
+__device__ __forceinline__ void cand_update(Cand& c, float v, uint32_t pos, uint32_t lvl) {
+    if (cand_better(v, pos, c)) {
+        c.v = v;
+        c.pos = pos;
+        c.lvl = lvl;
+    }
+}
+
+__device__ __forceinline__ float f_inf() { return __int_as_float(0x7f800000); }
+__device__ __forceinline__ float f_nan() { return __int_as_float(0x7fc00000); }
+
+}  // namespace rmq

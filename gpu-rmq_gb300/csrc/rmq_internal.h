@@ -1,0 +1,43 @@
+// rmq_internal.h — launchers shared between the kernel translation units and
+// the C ABI implementation.  Host-only declarations (no device code).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "rmq_common.cuh"
+
+namespace rmq {
+
+// Host level-layout rule (reference src/xxx.h:225-243, generalised to rf = 2^rf_log).
+Layout plan_layout(uint64_t n, uint64_t t, uint32_t rf_log);
+
+// Build level k+1 from level k for every k in [0, num_levels-1).
+// `val_buf`/`idx_buf` are the level buffers (layout.total entries each);
+// `idx_buf` may be null (no argmin support).
+cudaError_t launch_build(const Layout& lay, const float* d_values, float* val_buf,
+                         uint32_t* idx_buf, cudaStream_t s);
+
+struct QueryArgs {
+    Levels lv;
+    const uint2* qs;
+    uint32_t q;
+    float* out_min;      // may be null for argmin queries
+    uint32_t* out_idx;   // null for min queries
+    uint32_t* err;       // invalid-query counter or null
+    int variant;         // 1 = CL, 2 = VL
+    int lanes;           // CL tile width
+    uint32_t rf_log;
+    const void* persist_base;   // L2 access-policy window (null = none)
+    size_t persist_bytes;
+};
+
+cudaError_t launch_query(const QueryArgs& a, cudaStream_t s);
+
+cudaError_t launch_bruteforce(const float* vals, uint32_t n, const uint2* qs, uint32_t q,
+                              float* out_min, uint32_t* out_idx, cudaStream_t s);
+
+// Number of kernel launches the last launch_build issued (for accounting).
+int build_launch_count(const Layout& lay);
+
+}  // namespace rmq

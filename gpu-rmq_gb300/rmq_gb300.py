@@ -1,0 +1,299 @@
+"""Python binding of the GB300 RMQ C ABI (include/rmq_gb300.h) over ctypes.
+
+This is the host-side mirror used by the tests and bench.py.  The work is done
+by librmq_gb300.so (hand-written CUDA for sm_103a); this module only moves
+pointers and sizes across the C boundary.  There is no fallback: if the
+library is missing, every entry point raises.
+
+Reference mapping (reference files, by path within the reference project):
+  Hierarchy(...).query      xxx_rmq / hierarchical_vector_load (src/xxx.h:204, :933)
+  Hierarchy(...).query_idx  argmin over the hierarchy (new; results of
+                            gpu_rmq_basic_idx, src/cuda_methods.cuh:106)
+  bruteforce(...)           gpu_rmq_basic{,_idx} (src/cuda_methods.cuh:72-137)
+  gen_array / gen_queries   random_array_par_cpu / random_queries_par_cpu
+                            (src/rand.cuh:49-217)
+"""
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "librmq_gb300.so"
+GEN_PATH = PKG / "librmq_gen.so"
+
+RMQ_OK = 0
+RMQ_ERR_ARG = 1
+RMQ_ERR_CUDA = 2
+RMQ_ERR_OOM = 3
+RMQ_ERR_QUERY_RANGE = 4
+RMQ_ERR_TIMEOUT = 5
+RMQ_ERR_NO_INDEX = 6
+RMQ_ERR_UNSUPPORTED = 7
+
+VARIANT_AUTO = 0
+VARIANT_CL = 1
+VARIANT_VL = 2
+VARIANTS = {"auto": VARIANT_AUTO, "cl": VARIANT_CL, "vl": VARIANT_VL}
+
+NO_POS = 0xFFFFFFFF
+
+
+class RMQConfig(ctypes.Structure):
+    _fields_ = [
+        ("variant", ctypes.c_int32),
+        ("scan_threshold", ctypes.c_uint64),
+        ("rf_log", ctypes.c_int32),
+        ("lanes", ctypes.c_int32),
+        ("with_index", ctypes.c_int32),
+        ("l2_persist", ctypes.c_int32),
+        ("validate", ctypes.c_int32),
+    ]
+
+
+class RMQInfo(ctypes.Structure):
+    _fields_ = [
+        ("num_levels", ctypes.c_uint32),
+        ("rf_log", ctypes.c_uint32),
+        ("variant", ctypes.c_int32),
+        ("lanes", ctypes.c_int32),
+        ("n", ctypes.c_uint64),
+        ("scan_threshold", ctypes.c_uint64),
+        ("level_size", ctypes.c_uint64 * 20),
+        ("level_offset", ctypes.c_uint64 * 20),
+        ("level_bytes", ctypes.c_uint64),
+        ("build_ms", ctypes.c_float),
+    ]
+
+    def sizes(self) -> list[int]:
+        return [int(self.level_size[k]) for k in range(self.num_levels)]
+
+    def offsets(self) -> list[int]:
+        return [int(self.level_offset[k]) for k in range(self.num_levels)]
+
+
+class RMQError(RuntimeError):
+    def __init__(self, status: int, what: str):
+        self.status = status
+        super().__init__(f"{what}: {strerror(status)} (status {status})")
+
+
+_lib = None
+_gen = None
+
+_P = ctypes.c_void_p
+_U64 = ctypes.c_uint64
+
+
+def lib() -> ctypes.CDLL:
+    """Loads librmq_gb300.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with `python -c \"import __graft_entry__ as g; g.build()\"`")
+        L = ctypes.CDLL(str(LIB_PATH))
+        L.rmq_config_init.argtypes = [ctypes.POINTER(RMQConfig)]
+        L.rmq_config_init.restype = None
+        L.rmq_build.argtypes = [_P, _U64, ctypes.POINTER(RMQConfig), _P, ctypes.POINTER(_P)]
+        L.rmq_build.restype = ctypes.c_int
+        L.rmq_query.argtypes = [_P, _P, _U64, _P, _P]
+        L.rmq_query.restype = ctypes.c_int
+        L.rmq_query_idx.argtypes = [_P, _P, _U64, _P, _P, _P]
+        L.rmq_query_idx.restype = ctypes.c_int
+        L.rmq_scan_bruteforce.argtypes = [_P, _U64, _P, _U64, _P, _P, _P]
+        L.rmq_scan_bruteforce.restype = ctypes.c_int
+        L.rmq_get_info.argtypes = [_P, ctypes.POINTER(RMQInfo)]
+        L.rmq_get_info.restype = ctypes.c_int
+        L.rmq_destroy.argtypes = [_P]
+        L.rmq_destroy.restype = None
+        L.rmq_strerror.argtypes = [ctypes.c_int]
+        L.rmq_strerror.restype = ctypes.c_char_p
+        L.rmq_plan_layout.argtypes = [_U64, _U64, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(RMQInfo)]
+        L.rmq_plan_layout.restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def genlib() -> ctypes.CDLL:
+    global _gen
+    if _gen is None:
+        if not GEN_PATH.exists():
+            raise RuntimeError(f"{GEN_PATH} is missing: build the package first")
+        G = ctypes.CDLL(str(GEN_PATH))
+        G.rmq_gen_array.argtypes = [_U64, ctypes.c_int32, _P]
+        G.rmq_gen_array.restype = None
+        G.rmq_gen_queries.argtypes = [_U64, ctypes.c_int32, _U64, ctypes.c_int32, ctypes.c_int32, _P]
+        G.rmq_gen_queries.restype = ctypes.c_int32
+        G.rmq_gen_plant_min_ties.argtypes = [_P, _U64, ctypes.c_double, ctypes.c_int32]
+        G.rmq_gen_plant_min_ties.restype = None
+        G.rmq_gen_sample_indices.argtypes = [_U64, _U64, ctypes.c_int32, _P]
+        G.rmq_gen_sample_indices.restype = _U64
+        _gen = G
+    return _gen
+
+
+def strerror(status: int) -> str:
+    return lib().rmq_strerror(status).decode()
+
+
+def config(variant: str | int = "auto", t: int = 0, rf_log: int = 0, lanes: int = 0,
+           with_index: bool = True, l2_persist: bool = False, validate: bool = False) -> RMQConfig:
+    cfg = RMQConfig()
+    lib().rmq_config_init(ctypes.byref(cfg))
+    cfg.variant = VARIANTS[variant] if isinstance(variant, str) else int(variant)
+    cfg.scan_threshold = int(t)
+    cfg.rf_log = int(rf_log)
+    cfg.lanes = int(lanes)
+    cfg.with_index = 1 if with_index else 0
+    cfg.l2_persist = 1 if l2_persist else 0
+    cfg.validate = 1 if validate else 0
+    return cfg
+
+
+def plan_layout(n: int, t: int = 0, rf_log: int = 0, variant: str | int = "auto") -> RMQInfo:
+    """Level layout for n entries (host-only, no GPU needed)."""
+    info = RMQInfo()
+    v = VARIANTS[variant] if isinstance(variant, str) else int(variant)
+    st = lib().rmq_plan_layout(n, t, rf_log, v, ctypes.byref(info))
+    if st != RMQ_OK:
+        raise RMQError(st, "rmq_plan_layout")
+    return info
+
+
+def _stream_handle(stream) -> int:
+    if stream is None:
+        import torch
+        return torch.cuda.current_stream().cuda_stream
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream
+
+
+def _dev_ptr(t) -> int:
+    return int(t.data_ptr())
+
+
+class Hierarchy:
+    """A built hierarchy over a device-resident float32 tensor (torch)."""
+
+    def __init__(self, values, variant: str | int = "auto", t: int = 0, rf_log: int = 0,
+                 lanes: int = 0, with_index: bool = True, l2_persist: bool = False,
+                 validate: bool = False, stream=None):
+        import torch
+        if not isinstance(values, torch.Tensor) or values.device.type != "cuda":
+            raise TypeError("values must be a CUDA torch tensor")
+        if values.dtype != torch.float32 or not values.is_contiguous():
+            raise TypeError("values must be contiguous float32")
+        self.values = values  # level 0 is the caller's array: keep it alive
+        self.n = values.numel()
+        cfg = config(variant, t, rf_log, lanes, with_index, l2_persist, validate)
+        h = _P()
+        st = lib().rmq_build(_dev_ptr(values), self.n, ctypes.byref(cfg), _stream_handle(stream),
+                             ctypes.byref(h))
+        if st != RMQ_OK:
+            raise RMQError(st, "rmq_build")
+        self._h = h
+
+    @property
+    def handle(self) -> int:
+        return self._h.value
+
+    def info(self) -> RMQInfo:
+        info = RMQInfo()
+        st = lib().rmq_get_info(self._h, ctypes.byref(info))
+        if st != RMQ_OK:
+            raise RMQError(st, "rmq_get_info")
+        return info
+
+    def query_raw(self, lr_ptr: int, q: int, out_min_ptr: int, stream=None) -> int:
+        return lib().rmq_query(self._h, lr_ptr, q, out_min_ptr, _stream_handle(stream))
+
+    def query_idx_raw(self, lr_ptr: int, q: int, out_idx_ptr: int, out_min_ptr: int | None,
+                      stream=None) -> int:
+        return lib().rmq_query_idx(self._h, lr_ptr, q, out_idx_ptr, out_min_ptr or None,
+                                   _stream_handle(stream))
+
+    def query(self, lr, out=None, stream=None):
+        """Minima of the inclusive queries in lr (CUDA uint32/int32 tensor, shape [q, 2])."""
+        import torch
+        q = lr.numel() // 2
+        if out is None:
+            out = torch.empty(q, dtype=torch.float32, device=lr.device)
+        st = self.query_raw(_dev_ptr(lr), q, _dev_ptr(out), stream)
+        if st != RMQ_OK:
+            raise RMQError(st, "rmq_query")
+        return out
+
+    def query_idx(self, lr, out_idx=None, out_min=None, with_min: bool = False, stream=None):
+        import torch
+        q = lr.numel() // 2
+        if out_idx is None:
+            out_idx = torch.empty(q, dtype=torch.int32, device=lr.device)
+        if with_min and out_min is None:
+            out_min = torch.empty(q, dtype=torch.float32, device=lr.device)
+        st = self.query_idx_raw(_dev_ptr(lr), q, _dev_ptr(out_idx),
+                                _dev_ptr(out_min) if out_min is not None else None, stream)
+        if st != RMQ_OK:
+            raise RMQError(st, "rmq_query_idx")
+        return (out_idx, out_min) if with_min else out_idx
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            lib().rmq_destroy(self._h)
+            self._h = _P()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+def bruteforce(values, lr, want_min: bool = True, want_idx: bool = True, stream=None):
+    """The GPU brute-force checker (one warp per query)."""
+    import torch
+    q = lr.numel() // 2
+    out_min = torch.empty(q, dtype=torch.float32, device=lr.device) if want_min else None
+    out_idx = torch.empty(q, dtype=torch.int32, device=lr.device) if want_idx else None
+    st = lib().rmq_scan_bruteforce(_dev_ptr(values), values.numel(), _dev_ptr(lr), q,
+                                   _dev_ptr(out_min) if out_min is not None else None,
+                                   _dev_ptr(out_idx) if out_idx is not None else None,
+                                   _stream_handle(stream))
+    if st != RMQ_OK:
+        raise RMQError(st, "rmq_scan_bruteforce")
+    return out_min, out_idx
+
+
+# ---- host generators (librmq_gen.so) ----------------------------------------
+
+def gen_array(n: int, seed: int) -> np.ndarray:
+    a = np.empty(n, dtype=np.float32)
+    genlib().rmq_gen_array(n, seed, a.ctypes.data)
+    return a
+
+
+def gen_queries(q: int, lr: int, n: int, seed: int, trivial: bool = False) -> np.ndarray:
+    out = np.empty((q, 2), dtype=np.uint32)
+    rc = genlib().rmq_gen_queries(q, lr, n, seed, 1 if trivial else 0, out.ctypes.data)
+    if rc != 0:
+        raise ValueError(f"unknown length law lr={lr} for n={n}")
+    return out
+
+
+def plant_min_ties(a: np.ndarray, frac: float, seed: int) -> np.ndarray:
+    genlib().rmq_gen_plant_min_ties(a.ctypes.data, a.size, frac, seed)
+    return a
+
+
+def sample_indices(original_size: int, sample_size: int, seed: int) -> np.ndarray:
+    out = np.empty(min(original_size, sample_size), dtype=np.uint32)
+    m = genlib().rmq_gen_sample_indices(original_size, sample_size, seed, out.ctypes.data)
+    return out[:m]

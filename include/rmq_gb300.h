@@ -1,0 +1,130 @@
+/*
+ * rmq_gb300.h — C ABI of the GB300-native hierarchical range-minimum library.
+ *
+ * A handle holds a multi-level block-minimum structure over a caller-owned
+ * fp32 array that stays resident in device memory.  Queries are inclusive
+ * index pairs {l, r} (uint2 layout: 8 bytes per query, l first) and are
+ * answered on the device, stream-ordered, into caller-provided device buffers.
+ *
+ * Semantics (identical to the reference's brute-force scan):
+ *   min(l, r)    = A[argmin(l, r)]  (the bits of that element are returned)
+ *   argmin(l, r) = lowest i in [l, r] such that no j in [l, r] has A[j] < A[i]
+ *                  (IEEE-754 "<", so ties, including -0.0 vs +0.0, go to the
+ *                  lowest index).
+ * Inputs holding NaN are outside the contract.  A query with l > r or r >= n
+ * is invalid: its min is written as NaN and its argmin as 0xFFFFFFFF, and with
+ * cfg.validate set the call reports RMQ_ERR_QUERY_RANGE.
+ *
+ * No entry point exits the process or traps the GPU; all return a status.
+ * rmq_query / rmq_query_idx do not allocate, do not synchronise (unless
+ * cfg.validate is set) and may be issued concurrently on different streams:
+ * a handle is immutable after rmq_build returns.
+ */
+#ifndef RMQ_GB300_H
+#define RMQ_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* CUDA stream handle without pulling in the CUDA headers (same type as cudaStream_t). */
+typedef struct CUstream_st* rmq_stream_t;
+
+typedef struct rmq_handle rmq_handle;
+
+typedef enum {
+    RMQ_OK = 0,
+    RMQ_ERR_ARG = 1,          /* bad argument (null pointer, bad alignment, bad config) */
+    RMQ_ERR_CUDA = 2,         /* a CUDA runtime call failed */
+    RMQ_ERR_OOM = 3,          /* device allocation failed */
+    RMQ_ERR_QUERY_RANGE = 4,  /* at least one query had l > r or r >= n (validate mode) */
+    RMQ_ERR_TIMEOUT = 5,      /* a bounded device-side wait gave up */
+    RMQ_ERR_NO_INDEX = 6,     /* argmin asked of a handle built with with_index = 0 */
+    RMQ_ERR_UNSUPPORTED = 7   /* size or configuration outside what this build supports */
+} rmq_status;
+
+typedef enum {
+    RMQ_VARIANT_AUTO = 0,  /* pick by array size / threshold (tuned table)            */
+    RMQ_VARIANT_CL = 1,    /* lane-group cooperative scans (reference alg 16 family)  */
+    RMQ_VARIANT_VL = 2     /* one thread per query, 256-bit loads (reference alg 20)  */
+} rmq_variant;
+
+typedef struct {
+    int32_t  variant;         /* rmq_variant                                                    */
+    uint64_t scan_threshold;  /* t: build levels while a level holds more than t entries (0 = variant default) */
+    int32_t  rf_log;          /* log2 of the per-level reduction factor, 3..5 (0 = variant default)       */
+    int32_t  lanes;           /* CL: lanes cooperating on one query, 4/8/16/32 (0 = default)            */
+    int32_t  with_index;      /* build the per-block argmin arrays (needed by rmq_query_idx)             */
+    int32_t  l2_persist;      /* put the coarse levels in an L2 persisting access-policy window          */
+    int32_t  validate;        /* count invalid queries on the device; query calls then synchronise       */
+} rmq_config;
+
+typedef struct {
+    uint32_t num_levels;        /* including level 0 (the caller's array)               */
+    uint32_t rf_log;            /* reduction factor of every level step                 */
+    int32_t  variant;           /* resolved variant (never AUTO)                         */
+    int32_t  lanes;             /* resolved lanes per query (CL)                         */
+    uint64_t n;                 /* number of values                                      */
+    uint64_t scan_threshold;    /* resolved t                                            */
+    uint64_t level_size[20];    /* entries per level                                     */
+    uint64_t level_offset[20];  /* element offset of level k >= 1 in the level buffer    */
+    uint64_t level_bytes;       /* device bytes of level values (+ argmin arrays)        */
+    float    build_ms;          /* device time of the last build (CUDA events)           */
+} rmq_info;
+
+/* Fills *cfg with the defaults: AUTO variant, default t and rf, with_index = 1,
+ * l2_persist = 0, validate = 0. */
+void rmq_config_init(rmq_config* cfg);
+
+/* Builds the hierarchy over d_values[0..n) on `stream`.  d_values must be
+ * 32-byte aligned and must outlive the handle (level 0 is the caller's array).
+ * Replaces the build half of xxx_rmq (src/xxx.h:225-268) and of
+ * hierarchical_vector_load (src/xxx.h:958-1010).  Returns after the build is
+ * enqueued and its device time recorded (the call waits for the build). */
+int rmq_build(const float* d_values, uint64_t n, const rmq_config* cfg,
+              rmq_stream_t stream, rmq_handle** out);
+
+/* Range minima of q inclusive queries d_lr[2i] = l, d_lr[2i+1] = r into d_min[q].
+ * Replaces the query half of xxx_rmq (src/xxx.h:273-294, kernel src/xxx.h:124-200)
+ * and of hierarchical_vector_load (src/xxx.h:1012-1036, kernel src/xxx.h:883-930);
+ * the results are those of gpu_rmq_basic (src/cuda_methods.cuh:72). */
+int rmq_query(const rmq_handle* h, const uint32_t* d_lr, uint64_t q, float* d_min,
+              rmq_stream_t stream);
+
+/* Range argmin (lowest index on ties) into d_argmin[q]; also the minima into
+ * d_min_or_null when it is not NULL.  The reference has no hierarchical argmin;
+ * the results are those of gpu_rmq_basic_idx (src/cuda_methods.cuh:106) and
+ * cpu_rmq_idx (src/cpu_methods.h:56). */
+int rmq_query_idx(const rmq_handle* h, const uint32_t* d_lr, uint64_t q,
+                  uint32_t* d_argmin, float* d_min_or_null, rmq_stream_t stream);
+
+/* Brute-force scan, one thread per query (the reference's GPU checker,
+ * kernel_rmq_basic / kernel_rmq_basic_idx, src/cuda_methods.cuh:4-44).
+ * Either output may be NULL.  Used by the driver's --check and as alg 2/102. */
+int rmq_scan_bruteforce(const float* d_values, uint64_t n, const uint32_t* d_lr,
+                        uint64_t q, float* d_min_or_null, uint32_t* d_argmin_or_null,
+                        rmq_stream_t stream);
+
+/* Layout and build statistics of a handle. */
+int rmq_get_info(const rmq_handle* h, rmq_info* info);
+
+/* Frees the level buffers.  Safe on NULL.  Waits for work using the handle
+ * on the build stream. */
+void rmq_destroy(rmq_handle* h);
+
+/* Static, human-readable name of a status code. */
+const char* rmq_strerror(int status);
+
+/* Level layout only (host computation, no device work): the reference's rule
+ * (src/xxx.h:225-243) generalised to rf = 2^rf_log.  Returns RMQ_ERR_ARG when
+ * t is below the variant's minimum.  Usable without a GPU. */
+int rmq_plan_layout(uint64_t n, uint64_t scan_threshold, int32_t rf_log,
+                    int32_t variant, rmq_info* info);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RMQ_GB300_H */
