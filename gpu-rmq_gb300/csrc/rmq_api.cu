@@ -44,6 +44,10 @@ constexpr uint64_t kClT = 64;
 constexpr int kClLanes = 8;
 constexpr int kVlRfLog = 3;
 constexpr uint64_t kVlT = 32;
+// AUTO resolves to VL with rf = 8: measured on GB300 it is the fastest
+// work distribution at every batch size and array size tried (the
+// level-parallel CL kernel replicates the descent's index arithmetic on every
+// lane of the tile, which costs more than the memory round trips it saves).
 
 // Largest supported n: queries are uint32 pairs and the descent rounds r up by
 // at most rf - 1 without overflowing 32 bits.

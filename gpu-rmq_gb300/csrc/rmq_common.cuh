@@ -62,6 +62,12 @@ __device__ __forceinline__ void ld_sector_policy(const float* p, float (&v)[8], 
         : "l"(p), "l"(pol));
 }
 
+__device__ __forceinline__ float fmin3(float a, float b, float c) {
+    float d;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+
 __device__ __forceinline__ void ld_quad(const float* p, float (&v)[4]) {
     asm("ld.global.nc.L1::no_allocate.v4.f32 {%0,%1,%2,%3}, [%4];"
                  : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3])
@@ -80,23 +86,42 @@ __device__ __forceinline__ uint64_t policy_evict_first() {
     return pol;
 }
 
+#ifndef RMQ_Q_HINT
+#define RMQ_Q_HINT 0  // query stream: 0 = evict_first, 1 = default
+#endif
+#ifndef RMQ_ST_HINT
+#define RMQ_ST_HINT 0  // result stores: 0 = .cs (streaming), 1 = default
+#endif
+
 // Streaming query load of one {l, r} pair; the query array is read once, so
 // it is marked evict-first in L2 to leave room for the coarse levels.
 __device__ __forceinline__ uint2 ld_query(const uint2* p) {
     uint2 v;
+#if RMQ_Q_HINT == 0
     asm(
         "{\n\t.reg .b64 pol;\n\t"
         "createpolicy.fractional.L2::evict_first.b64 pol, 1.0;\n\t"
         "ld.global.nc.L1::no_allocate.L2::cache_hint.v2.u32 {%0,%1}, [%2], pol;\n\t}"
         : "=r"(v.x), "=r"(v.y) : "l"(p));
+#else
+    v = __ldg(p);
+#endif
     return v;
 }
 
 __device__ __forceinline__ void st_stream(float* p, float v) {
+#if RMQ_ST_HINT == 0
     asm volatile("st.global.cs.f32 [%0], %1;" :: "l"(p), "f"(v) : "memory");
+#else
+    *p = v;
+#endif
 }
 __device__ __forceinline__ void st_stream(uint32_t* p, uint32_t v) {
+#if RMQ_ST_HINT == 0
     asm volatile("st.global.cs.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
+#else
+    *p = v;
+#endif
 }
 
 // ---------------------------------------------------------------------------

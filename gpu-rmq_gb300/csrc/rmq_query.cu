@@ -11,269 +11,504 @@
 // Two work distributions share that descent:
 //   VL  one thread per query, 256-bit sector loads (reference alg 20,
 //       kernel_hierarchical_vector_load, src/xxx.h:883-930, which uses float4);
-//   CL  a tile of G lanes per query with 128-bit loads; the tile's G queries
-//       are loaded coalesced, one per lane, broadcast by shuffle and answered
-//       one after the other (reference alg 16, xxx_query, src/xxx.h:124-200).
+//   CL  a tile of G lanes per query (reference alg 16, xxx_query,
+//       src/xxx.h:124-200, where a tile answers its queries one after the
+//       other); here the lanes split the query's pieces by level so all
+//       loads of one query are in flight together.
 #include "rmq_internal.h"
 
 namespace rmq {
 
 // ---------------------------------------------------------------------------
 // VL: thread per query
+//
+// Phase 1 takes the minimum over all pieces with a masked 8-wide min per
+// 32-byte sector (one 256-bit load each).  For argmin it also remembers, at
+// sector granularity, where that minimum was first seen: left pieces and the
+// final piece are visited in ascending position order (strict "<" keeps the
+// first), right pieces in descending order ("<=" lets the more-left sector
+// win), and a left/final winner beats a right winner on equal values.
+// Phase 2 re-reads only the winning sector, takes its first entry equal to the
+// minimum and, for a coarse level, loads that entry's stored level-0 index.
 // ---------------------------------------------------------------------------
+
+// L2 eviction priorities (tuning knobs; 0 selects the default shown).
+#ifndef RMQ_L0_HINT
+#define RMQ_L0_HINT 0  // level-0 sectors: 0 = evict_first, 1 = evict_normal
+#endif
+#ifndef RMQ_UP_HINT
+#define RMQ_UP_HINT 0  // coarse-level sectors: 0 = evict_last, 1 = evict_normal
+#endif
+#ifndef RMQ_IDX_HINT
+#define RMQ_IDX_HINT 0  // argmin index lookups: 0 = evict_last, 1 = evict_normal
+#endif
+
+struct L2Policies {
+    uint64_t fine;    // level 0: read once per query
+    uint64_t coarse;  // levels >= 1: shared by all queries
+};
+
+__device__ __forceinline__ uint64_t policy_evict_normal() {
+    uint64_t pol;
+    asm volatile("createpolicy.fractional.L2::evict_normal.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+
+__device__ __forceinline__ L2Policies make_policies() {
+    return L2Policies{RMQ_L0_HINT == 0 ? policy_evict_first() : policy_evict_normal(),
+                      RMQ_UP_HINT == 0 ? policy_evict_last() : policy_evict_normal()};
+}
+
+__device__ __forceinline__ uint32_t ld_index(const uint32_t* p) {
+#if RMQ_IDX_HINT == 0
+    uint32_t v;
+    asm("{\n\t.reg .b64 pol;\n\t"
+        "createpolicy.fractional.L2::evict_last.b64 pol, 1.0;\n\t"
+        "ld.global.nc.L2::cache_hint.u32 %0, [%1], pol;\n\t}"
+        : "=r"(v) : "l"(p));
+    return v;
+#else
+    return __ldg(p);
+#endif
+}
 
 // Loads the sector starting at s of level k.  Level 0 is the caller's array,
 // which is not padded: a sector that crosses its end is read element-wise.
-__device__ __forceinline__ void load_level_sector(const float* base, uint32_t size, uint32_t k,
-                                                  uint32_t s, float (&v)[8]) {
-    if (k > 0 || s + 8u <= size) {
-        ld_sector(base + s, v);
+__device__ __forceinline__ void load_level_sector(const Levels& lv, uint32_t k, uint32_t s,
+                                                  const L2Policies& pol, float (&v)[8]) {
+    const float* base = lv.val[k];
+    if (k > 0) {
+        ld_sector_policy(base + s, v, pol.coarse);
+    } else if (s + 8u <= lv.size[0]) {
+        ld_sector_policy(base + s, v, pol.fine);
     } else {
+        const uint32_t size = lv.size[0];
 #pragma unroll
         for (int j = 0; j < 8; ++j) v[j] = (s + j < size) ? base[s + j] : f_inf();
     }
 }
 
-// Candidate scan of [lo, hi) at level k (thread-private).
-__device__ __forceinline__ void vl_scan_cand(const Levels& lv, uint32_t k, uint32_t shift,
-                                             uint32_t lo, uint32_t hi, Cand& c) {
-    const float* base = lv.val[k];
-    const uint32_t size = lv.size[k];
-    for (uint32_t s = lo & ~7u; s < hi; s += 8u) {
-        float v[8];
-        load_level_sector(base, size, k, s, v);
+// Minimum of v[j] for jlo <= j < jhi (+inf if empty).
+__device__ __forceinline__ float sector_min(const float (&v)[8], uint32_t jlo, uint32_t jhi) {
+    float w[8];
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            const uint32_t e = s + j;
-            if (e >= lo && e < hi) cand_update(c, v[j], e << shift, k);
+    for (int j = 0; j < 8; ++j) w[j] = (uint32_t(j) >= jlo && uint32_t(j) < jhi) ? v[j] : f_inf();
+    const float a = fmin3(w[0], w[1], w[2]);
+    const float b = fmin3(w[3], w[4], w[5]);
+    return fmin3(a, b, fminf(w[6], w[7]));
+}
+
+// Sector-granular position of the first minimum.  meta packs the level
+// (bits 0-7), jlo (bits 8-15) and jhi (bits 16-23); kNoPos = none yet.
+struct Tracker {
+    float v;
+    uint32_t s;
+    uint32_t meta;
+};
+
+__device__ __forceinline__ void tracker_init(Tracker& t) {
+    t.v = f_inf();
+    t.s = 0;
+    t.meta = kNoPos;
+}
+
+template <bool ARGMIN, bool RIGHT>
+__device__ __forceinline__ void scan_sector(const Levels& lv, uint32_t k, uint32_t s, uint32_t jlo,
+                                            uint32_t jhi, const L2Policies& pol, float& m, Tracker& t) {
+    float v[8];
+    load_level_sector(lv, k, s, pol, v);
+    const float sm = sector_min(v, jlo, jhi);
+    m = fminf(m, sm);
+    if (ARGMIN) {
+        const bool take = RIGHT ? (sm <= t.v) : (sm < t.v);
+        if (take) {
+            t.v = sm;
+            t.s = s;
+            t.meta = k | (jlo << 8) | (jhi << 16);
         }
     }
 }
 
-// Minimum-only scan of [lo, hi) at level k.
-__device__ __forceinline__ float vl_scan_min(const Levels& lv, uint32_t k, uint32_t lo, uint32_t hi,
-                                             float m) {
-    const float* base = lv.val[k];
-    const uint32_t size = lv.size[k];
+// Ascending scan of [lo, hi) (lo < hi) at level k, sector by sector.
+template <bool ARGMIN>
+__device__ __forceinline__ void scan_fwd(const Levels& lv, uint32_t k, uint32_t lo, uint32_t hi,
+                                         const L2Policies& pol, float& m, Tracker& t) {
     for (uint32_t s = lo & ~7u; s < hi; s += 8u) {
-        float v[8];
-        load_level_sector(base, size, k, s, v);
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            const uint32_t e = s + j;
-            m = fminf(m, (e >= lo && e < hi) ? v[j] : f_inf());
+        const uint32_t jlo = s < lo ? lo - s : 0u;
+        const uint32_t jhi = hi - s < 8u ? hi - s : 8u;
+        scan_sector<ARGMIN, false>(lv, k, s, jlo, jhi, pol, m, t);
+    }
+}
+
+// Descending scan of [lo, hi) (lo < hi) at level k (right pieces).
+template <bool ARGMIN>
+__device__ __forceinline__ void scan_bwd(const Levels& lv, uint32_t k, uint32_t lo, uint32_t hi,
+                                         const L2Policies& pol, float& m, Tracker& t) {
+    const uint32_t first = lo & ~7u;
+    for (uint32_t s = (hi - 1u) & ~7u;; s -= 8u) {
+        const uint32_t jlo = s < lo ? lo - s : 0u;
+        const uint32_t jhi = hi - s < 8u ? hi - s : 8u;
+        scan_sector<ARGMIN, true>(lv, k, s, jlo, jhi, pol, m, t);
+        if (s == first) break;
+    }
+}
+
+// Final pieces longer than this many entries (only possible at the top level,
+// whose size is bounded by t) are scanned by the whole warp instead of one lane.
+constexpr uint32_t kLongScan = 64;
+
+// Phase 1 up to (not including) the final piece; returns the running minimum
+// and leaves the final piece [l, r) at level k in the arguments.
+template <int R, bool ARGMIN>
+__device__ __forceinline__ float vl_descend(const Levels& lv, uint32_t& l, uint32_t& r, uint32_t& k,
+                                            const L2Policies& pol, Tracker& tl, Tracker& tr) {
+    constexpr uint32_t RF = 1u << R;
+    float m = f_inf();
+    k = 0;
+    while (k + 1 < lv.num_levels && r - l > 2u * RF) {
+        const uint32_t nl = (l + RF - 1) & ~(RF - 1);
+        const uint32_t pr = r & ~(RF - 1);
+        if (R == 3) {
+            // rf = 8: each boundary piece is exactly one sector; issue both loads first.
+            float a[8], b[8];
+            const bool has_l = nl > l, has_r = r > pr;
+            if (has_l) load_level_sector(lv, k, l & ~7u, pol, a);
+            if (has_r) load_level_sector(lv, k, pr, pol, b);
+            if (has_l) {
+                const float sm = sector_min(a, l & 7u, 8u);
+                m = fminf(m, sm);
+                if (ARGMIN && sm < tl.v) {
+                    tl.v = sm;
+                    tl.s = l & ~7u;
+                    tl.meta = k | ((l & 7u) << 8) | (8u << 16);
+                }
+            }
+            if (has_r) {
+                const float sm = sector_min(b, 0u, r - pr);
+                m = fminf(m, sm);
+                if (ARGMIN && sm <= tr.v) {
+                    tr.v = sm;
+                    tr.s = pr;
+                    tr.meta = k | ((r - pr) << 16);
+                }
+            }
+        } else {
+            if (nl > l) scan_fwd<ARGMIN>(lv, k, l, nl, pol, m, tl);
+            if (r > pr) scan_bwd<ARGMIN>(lv, k, pr, r, pol, m, tr);
         }
+        l = nl >> R;
+        r = pr >> R;
+        ++k;
     }
     return m;
 }
 
-template <int R>
-__device__ __forceinline__ Cand vl_descend_cand(const Levels& lv, uint32_t l, uint32_t r) {
-    constexpr uint32_t RF = 1u << R;
-    Cand c;
-    cand_init(c);
-    uint32_t k = 0;
-    while (k + 1 < lv.num_levels && r - l > 2u * RF) {
-        const uint32_t nl = (l + RF - 1) & ~(RF - 1);
-        const uint32_t pr = r & ~(RF - 1);
-        const uint32_t shift = k * R;
-        if (nl > l) vl_scan_cand(lv, k, shift, l, nl, c);
-        if (r > pr) vl_scan_cand(lv, k, shift, pr, r, c);
-        l = nl >> R;
-        r = pr >> R;
-        ++k;
+// Whole-warp scan of the final piece [lo, hi) of level k owned by lane
+// `owner`: lane j reads sectors j, j + 32, ... of the piece (1 KiB contiguous
+// per warp load), keeps its first sector holding its minimum, and the warp
+// combines by (value, sector start) so the first sector holding the piece
+// minimum wins; the owner merges it into its running minimum and tracker.
+template <bool ARGMIN>
+__device__ __forceinline__ void warp_scan_final(const Levels& lv, uint32_t k, uint32_t lo, uint32_t hi,
+                                                uint32_t owner, const L2Policies& pol, float& m, Tracker& tl) {
+    const uint32_t lane = threadIdx.x & 31u;
+    float best = f_inf();
+    uint32_t bs = kNoPos;
+    for (uint32_t s = (lo & ~7u) + 8u * lane; s < hi; s += 256u) {
+        const uint32_t jlo = s < lo ? lo - s : 0u;
+        const uint32_t jhi = hi - s < 8u ? hi - s : 8u;
+        float v[8];
+        load_level_sector(lv, k, s, pol, v);
+        const float sm = sector_min(v, jlo, jhi);
+        if (bs == kNoPos || sm < best) {
+            best = sm;
+            bs = s;
+        }
     }
-    vl_scan_cand(lv, k, k * R, l, r, c);
-    return c;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float ov = __shfl_xor_sync(0xffffffffu, best, o);
+        const uint32_t os = __shfl_xor_sync(0xffffffffu, bs, o);
+        if (os != kNoPos && (bs == kNoPos || ov < best || (ov == best && os < bs))) {
+            best = ov;
+            bs = os;
+        }
+    }
+    if (lane == owner) {
+        m = fminf(m, best);
+        if (ARGMIN && best < tl.v) {
+            tl.v = best;
+            tl.s = bs;
+            const uint32_t jlo = bs < lo ? lo - bs : 0u;
+            const uint32_t jhi = hi - bs < 8u ? hi - bs : 8u;
+            tl.meta = k | (jlo << 8) | (jhi << 16);
+        }
+    }
 }
 
-template <int R>
-__device__ __forceinline__ float vl_descend_min(const Levels& lv, uint32_t l, uint32_t r) {
-    constexpr uint32_t RF = 1u << R;
+// Phase 1 for every lane of the warp (all 32 lanes must call it): private
+// descent and short final scans, then the warp's long final scans one by one.
+template <int R, bool ARGMIN>
+__device__ __forceinline__ float vl_phase1(const Levels& lv, bool active, uint32_t l, uint32_t r,
+                                           const L2Policies& pol, Tracker& tl, Tracker& tr) {
     float m = f_inf();
     uint32_t k = 0;
-    while (k + 1 < lv.num_levels && r - l > 2u * RF) {
-        const uint32_t nl = (l + RF - 1) & ~(RF - 1);
-        const uint32_t pr = r & ~(RF - 1);
-        if (nl > l) m = vl_scan_min(lv, k, l, nl, m);
-        if (r > pr) m = vl_scan_min(lv, k, pr, r, m);
-        l = nl >> R;
-        r = pr >> R;
-        ++k;
+    bool is_long = false;
+    if (active) {
+        m = vl_descend<R, ARGMIN>(lv, l, r, k, pol, tl, tr);
+        if (r - l <= kLongScan) scan_fwd<ARGMIN>(lv, k, l, r, pol, m, tl);
+        else is_long = true;
     }
-    return vl_scan_min(lv, k, l, r, m);
+    uint32_t pending = __ballot_sync(0xffffffffu, is_long);
+    while (pending != 0u) {
+        const uint32_t owner = uint32_t(__ffs(pending) - 1);
+        const uint32_t ok = __shfl_sync(0xffffffffu, k, owner);
+        const uint32_t olo = __shfl_sync(0xffffffffu, l, owner);
+        const uint32_t ohi = __shfl_sync(0xffffffffu, r, owner);
+        warp_scan_final<ARGMIN>(lv, ok, olo, ohi, owner, pol, m, tl);
+        pending &= pending - 1u;
+    }
+    return m;
 }
 
-// Level-0 index of a candidate (one dependent load for coarse-level winners).
+// Phase 2: first entry equal to the minimum inside the winning sector.
 template <int R>
-__device__ __forceinline__ uint32_t cand_index(const Levels& lv, const Cand& c, uint32_t l) {
-    if (c.pos == kNoPos) return l;  // only reachable with NaN inputs (out of contract)
-    if (c.lvl == 0) return c.pos;
-    return __ldg(lv.idx[c.lvl] + (c.pos >> (c.lvl * R)));
+__device__ __forceinline__ void vl_locate(const Levels& lv, uint32_t l, const Tracker& tl, const Tracker& tr,
+                                          const L2Policies& pol, float& out_v, uint32_t& out_i) {
+    const bool right = tr.v < tl.v;
+    const Tracker& w = right ? tr : tl;
+    if (w.meta == kNoPos) {
+        // No candidate compared below +inf: every entry is +inf (or NaN,
+        // outside the contract); the scan's answer is the first entry.
+        out_i = l;
+        out_v = __ldg(lv.val[0] + l);
+        return;
+    }
+    const uint32_t k = w.meta & 0xffu;
+    const uint32_t jlo = (w.meta >> 8) & 0xffu;
+    const uint32_t jhi = (w.meta >> 16) & 0xffu;
+    float v[8];
+    load_level_sector(lv, k, w.s, pol, v);
+    uint32_t j = jlo;
+#pragma unroll
+    for (int jj = 7; jj >= 0; --jj) {
+        if (uint32_t(jj) >= jlo && uint32_t(jj) < jhi && v[jj] == w.v) j = uint32_t(jj);
+    }
+    float val = v[0];
+#pragma unroll
+    for (int jj = 1; jj < 8; ++jj) val = (uint32_t(jj) == j) ? v[jj] : val;
+    const uint32_t e = w.s + j;
+    out_v = val;
+    out_i = k == 0 ? e : ld_index(lv.idx[k] + e);
 }
 
 template <int R, bool ARGMIN>
 __global__ void __launch_bounds__(256)
 query_vl_kernel(Levels lv, const uint2* __restrict__ qs, uint32_t q, float* __restrict__ out_min,
                 uint32_t* __restrict__ out_idx, uint32_t* __restrict__ err) {
+    // No early return: every lane takes part in the warp's long final scans.
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= q) return;
-    const uint2 Q = ld_query(qs + i);
-    if (Q.x > Q.y || Q.y >= lv.size[0]) {
+    const bool in_range = i < q;
+    uint2 Q = make_uint2(1u, 0u);
+    if (in_range) Q = ld_query(qs + i);
+    const bool valid = in_range && Q.x <= Q.y && Q.y < lv.size[0];
+    if (in_range && !valid) {
         if (out_min != nullptr) st_stream(out_min + i, f_nan());
         if (ARGMIN) st_stream(out_idx + i, kNoPos);
         if (err != nullptr) atomicAdd(err, 1u);
-        return;
     }
+    const L2Policies pol = make_policies();
     const uint32_t l = Q.x, r = Q.y + 1;
+    Tracker tl, tr;
+    tracker_init(tl);
+    tracker_init(tr);
     if (ARGMIN) {
-        const Cand c = vl_descend_cand<R>(lv, l, r);
-        st_stream(out_idx + i, cand_index<R>(lv, c, l));
-        if (out_min != nullptr) st_stream(out_min + i, c.v);
+        vl_phase1<R, true>(lv, valid, l, r, pol, tl, tr);
+        if (valid) {
+            float v;
+            uint32_t idx;
+            vl_locate<R>(lv, l, tl, tr, pol, v, idx);
+            st_stream(out_idx + i, idx);
+            if (out_min != nullptr) st_stream(out_min + i, v);
+        }
     } else {
-        float m = vl_descend_min<R>(lv, l, r);
+        float m = vl_phase1<R, false>(lv, valid, l, r, pol, tl, tr);
         // A zero minimum may be -0.0 or +0.0; the reference returns the bits of
-        // the first occurrence, so redo the query with positions in that case.
-        if (m == 0.0f) m = vl_descend_cand<R>(lv, l, r).v;
-        st_stream(out_min + i, m);
-    }
-}
-
-// ---------------------------------------------------------------------------
-// CL: tile of G lanes per query
-// ---------------------------------------------------------------------------
-
-__device__ __forceinline__ void load_level_quad(const float* base, uint32_t size, uint32_t k,
-                                                uint32_t s, float (&v)[4]) {
-    if (k > 0 || s + 4u <= size) {
-        ld_quad(base + s, v);
-    } else {
-#pragma unroll
-        for (int j = 0; j < 4; ++j) v[j] = (s + j < size) ? base[s + j] : f_inf();
-    }
-}
-
-// The tile scans two ranges of level k (either may be empty) as one list of
-// aligned quads: quads of A first, then quads of B; lane `lane` takes quads
-// lane, lane + G, ...
-template <int G, bool CAND>
-__device__ __forceinline__ void cl_scan_pair(const Levels& lv, uint32_t k, uint32_t shift,
-                                             uint32_t alo, uint32_t ahi, uint32_t blo, uint32_t bhi,
-                                             uint32_t lane, Cand& c, float& m) {
-    const float* base = lv.val[k];
-    const uint32_t size = lv.size[k];
-    const uint32_t a0 = alo & ~3u;
-    const uint32_t na = ahi > alo ? ((ahi - a0 + 3u) >> 2) : 0u;
-    const uint32_t b0 = blo & ~3u;
-    const uint32_t nb = bhi > blo ? ((bhi - b0 + 3u) >> 2) : 0u;
-    const uint32_t total = na + nb;
-    for (uint32_t j = lane; j < total; j += G) {
-        const bool in_a = j < na;
-        const uint32_t s = in_a ? a0 + 4u * j : b0 + 4u * (j - na);
-        const uint32_t lo = in_a ? alo : blo;
-        const uint32_t hi = in_a ? ahi : bhi;
-        float v[4];
-        load_level_quad(base, size, k, s, v);
-#pragma unroll
-        for (int t = 0; t < 4; ++t) {
-            const uint32_t e = s + t;
-            const bool inside = e >= lo && e < hi;
-            if (CAND) {
-                if (inside) cand_update(c, v[t], e << shift, k);
-            } else {
-                m = fminf(m, inside ? v[t] : f_inf());
+        // the first occurrence, so locate it (warp-uniform participation).
+        const bool zero = valid && m == 0.0f;
+        if (__any_sync(0xffffffffu, zero)) {
+            vl_phase1<R, true>(lv, zero, l, r, pol, tl, tr);
+            if (zero) {
+                uint32_t idx;
+                vl_locate<R>(lv, l, tl, tr, pol, m, idx);
             }
         }
+        if (valid) st_stream(out_min + i, m);
     }
 }
 
-template <int R, int G, bool CAND>
-__device__ __forceinline__ void cl_descend(const Levels& lv, uint32_t l, uint32_t r, uint32_t lane,
-                                           Cand& c, float& m) {
+// ---------------------------------------------------------------------------
+// CL: a tile of G lanes per query, level-parallel
+//
+// Lane j of the tile owns the pieces of side (j & 1) (0 = left, 1 = right) at
+// levels j/2, j/2 + G/2, ... and the sectors j, j + G, ... of the final piece.
+// Every lane derives the descent (pure index arithmetic, no loads), then all
+// of its loads are issued together, so a query costs one memory round trip
+// for all levels instead of one per level.  The tile combines lane results by
+// (value, order key), where the key orders pieces by position: left pieces by
+// ascending level, then the final piece's sectors, then right pieces by
+// descending level; the lowest key among equal values is the first
+// occurrence.  The winning lane re-reads its sector, takes its first entry
+// equal to the minimum and, for a coarse level, loads the stored index.
+// ---------------------------------------------------------------------------
+constexpr uint32_t kKeyNone = 0xFFFFFFFFu;
+constexpr uint32_t kKeyFinal = 64u;  // keys of final sectors start here (levels < 20)
+
+struct LaneBest {
+    float v;
+    uint32_t key;
+    uint32_t s;     // sector start
+    uint32_t meta;  // level | jlo << 8 | jhi << 16
+};
+
+template <bool ARGMIN>
+__device__ __forceinline__ void lane_take(LaneBest& b, float sm, uint32_t key, uint32_t s, uint32_t meta) {
+    if (ARGMIN) {
+        if (sm < b.v || (sm == b.v && key < b.key)) {
+            b.v = sm;
+            b.key = key;
+            b.s = s;
+            b.meta = meta;
+        }
+    } else {
+        b.v = fminf(b.v, sm);
+    }
+}
+
+// One sector of level k restricted to [lo, hi).
+template <bool ARGMIN>
+__device__ __forceinline__ void cl_sector(const Levels& lv, uint32_t k, uint32_t s, uint32_t lo, uint32_t hi,
+                                          uint32_t key, const L2Policies& pol, LaneBest& b) {
+    const uint32_t jlo = s < lo ? lo - s : 0u;
+    const uint32_t jhi = hi - s < 8u ? hi - s : 8u;
+    float v[8];
+    load_level_sector(lv, k, s, pol, v);
+    lane_take<ARGMIN>(b, sector_min(v, jlo, jhi), key, s, k | (jlo << 8) | (jhi << 16));
+}
+
+template <int R, int G, bool ARGMIN>
+__device__ __forceinline__ void cl_lane_work(const Levels& lv, uint32_t l, uint32_t r, uint32_t lane,
+                                             const L2Policies& pol, LaneBest& b) {
     constexpr uint32_t RF = 1u << R;
+    constexpr uint32_t PAIRS = G / 2u;
+    const uint32_t my_level = lane >> 1;
+    const bool right = (lane & 1u) != 0u;
+    // Descent: stop level s and final piece [l, r) at level s; this lane's
+    // boundary pieces are recorded as they are passed (at most
+    // ceil(19 / PAIRS) of them; pieces are processed after the loop).
+    constexpr uint32_t kMaxPieces = (19u + PAIRS - 1u) / PAIRS;
+    uint32_t plo[kMaxPieces], phi[kMaxPieces];
+    uint32_t np = 0;
     uint32_t k = 0;
     while (k + 1 < lv.num_levels && r - l > 2u * RF) {
         const uint32_t nl = (l + RF - 1) & ~(RF - 1);
         const uint32_t pr = r & ~(RF - 1);
-        cl_scan_pair<G, CAND>(lv, k, k * R, l, nl, pr, r, lane, c, m);
+        if (k % PAIRS == my_level) {
+#pragma unroll
+            for (uint32_t i = 0; i < kMaxPieces; ++i) {  // constant indices keep plo/phi in registers
+                if (np == i) {
+                    plo[i] = right ? pr : l;
+                    phi[i] = right ? r : nl;
+                }
+            }
+            ++np;
+        }
         l = nl >> R;
         r = pr >> R;
         ++k;
     }
-    cl_scan_pair<G, CAND>(lv, k, k * R, l, r, 0u, 0u, lane, c, m);
-}
-
-template <int G>
-__device__ __forceinline__ void cl_reduce_cand(Cand& c, uint32_t mask) {
-#pragma unroll
-    for (int o = 1; o < G; o <<= 1) {
-        const float ov = __shfl_xor_sync(mask, c.v, o, G);
-        const uint32_t op = __shfl_xor_sync(mask, c.pos, o, G);
-        const uint32_t ol = __shfl_xor_sync(mask, c.lvl, o, G);
-        cand_update(c, ov, op, ol);
+    // Final piece sectors: all independent of the pieces, issued alongside.
+    const uint32_t f0 = l & ~7u;
+    for (uint32_t s = f0 + 8u * lane; s < r; s += 8u * G) {
+        cl_sector<ARGMIN>(lv, k, s, l, r, kKeyFinal + ((s - f0) >> 3), pol, b);
     }
-}
-
-template <int G>
-__device__ __forceinline__ float cl_reduce_min(float m, uint32_t mask) {
 #pragma unroll
-    for (int o = 1; o < G; o <<= 1) m = fminf(m, __shfl_xor_sync(mask, m, o, G));
-    return m;
+    for (uint32_t i = 0; i < kMaxPieces; ++i) {
+        if (i < np && phi[i] > plo[i]) {
+            const uint32_t lvl = my_level + i * PAIRS;
+            const uint32_t key = right ? (kKeyNone - 1u - lvl) : lvl;
+            for (uint32_t s = plo[i] & ~7u; s < phi[i]; s += 8u)
+                cl_sector<ARGMIN>(lv, lvl, s, plo[i], phi[i], key, pol, b);
+        }
+    }
 }
 
 template <int R, int G, bool ARGMIN>
 __global__ void __launch_bounds__(256)
 query_cl_kernel(Levels lv, const uint2* __restrict__ qs, uint32_t q, float* __restrict__ out_min,
                 uint32_t* __restrict__ out_idx, uint32_t* __restrict__ err) {
-    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t lane = threadIdx.x & (G - 1);
+    const uint32_t lane = threadIdx.x & (G - 1u);
+    const uint32_t qi = (blockIdx.x * blockDim.x + threadIdx.x) / G;
     const uint32_t wl = threadIdx.x & 31u;
     const uint32_t mask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (wl - lane));
-    const uint32_t n = lv.size[0];
-
-    uint2 Q = make_uint2(1u, 0u);
-    if (tid < q) Q = ld_query(qs + tid);
-    const bool valid = tid < q && Q.x <= Q.y && Q.y < n;
-    if (tid < q && !valid && err != nullptr) atomicAdd(err, 1u);
-
-    float my_min = f_nan();
-    Cand my_c;
-    cand_init(my_c);
-
-    for (int j = 0; j < G; ++j) {
-        const uint32_t l = __shfl_sync(mask, Q.x, j, G);
-        const uint32_t r = __shfl_sync(mask, Q.y, j, G) + 1u;
-        const bool v = __shfl_sync(mask, valid ? 1u : 0u, j, G) != 0u;
-        if (!v) continue;  // uniform across the tile
-        Cand c;
-        cand_init(c);
-        float m = f_inf();
-        if (ARGMIN) {
-            cl_descend<R, G, true>(lv, l, r, lane, c, m);
-            cl_reduce_cand<G>(c, mask);
-            if (lane == uint32_t(j)) {
-                my_c = c;
-                my_min = c.v;
-            }
-        } else {
-            cl_descend<R, G, false>(lv, l, r, lane, c, m);
-            m = cl_reduce_min<G>(m, mask);
-            if (m == 0.0f) {  // signed-zero tie: take the bits of the first occurrence
-                cand_init(c);
-                cl_descend<R, G, true>(lv, l, r, lane, c, m);
-                cl_reduce_cand<G>(c, mask);
-                m = c.v;
-            }
-            if (lane == uint32_t(j)) my_min = m;
+    if (qi >= q) return;  // uniform across the tile
+    const uint2 Q = ld_query(qs + qi);
+    if (Q.x > Q.y || Q.y >= lv.size[0]) {
+        if (lane == 0) {
+            if (out_min != nullptr) st_stream(out_min + qi, f_nan());
+            if (ARGMIN) st_stream(out_idx + qi, kNoPos);
+            if (err != nullptr) atomicAdd(err, 1u);
         }
+        return;
     }
-    if (tid < q) {
-        if (ARGMIN) {
-            const uint32_t idx = valid ? cand_index<R>(lv, my_c, Q.x) : kNoPos;
-            st_stream(out_idx + tid, idx);
-            if (out_min != nullptr) st_stream(out_min + tid, valid ? my_min : f_nan());
-        } else {
-            st_stream(out_min + tid, my_min);
+    const L2Policies pol = make_policies();
+    const uint32_t l = Q.x, r = Q.y + 1;
+    LaneBest b{f_inf(), kKeyNone, 0u, 0u};
+    bool need_locate = ARGMIN;
+    cl_lane_work<R, G, ARGMIN>(lv, l, r, lane, pol, b);
+    float m = b.v;
+#pragma unroll
+    for (int o = 1; o < G; o <<= 1) m = fminf(m, __shfl_xor_sync(mask, m, o, G));
+    if (!ARGMIN) {
+        if (m != 0.0f) {
+            if (lane == 0) st_stream(out_min + qi, m);
+            return;
+        }
+        // A zero minimum may be -0.0 or +0.0: locate the first one for its bits.
+        b = LaneBest{f_inf(), kKeyNone, 0u, 0u};
+        cl_lane_work<R, G, true>(lv, l, r, lane, pol, b);
+        need_locate = true;
+    }
+    if (need_locate) {
+        // The winner: lowest key among the lanes holding the minimum.
+        uint32_t key = (b.v == m) ? b.key : kKeyNone;
+#pragma unroll
+        for (int o = 1; o < G; o <<= 1) key = min(key, __shfl_xor_sync(mask, key, o, G));
+        if (key == kKeyNone) {
+            // No entry compared equal to the minimum: NaN inputs only (outside
+            // the contract); the scan's answer is the first entry.
+            if (lane == 0) {
+                if (out_idx != nullptr) st_stream(out_idx + qi, l);
+                if (out_min != nullptr) st_stream(out_min + qi, __ldg(lv.val[0] + l));
+            }
+            return;
+        }
+        if (b.key == key && b.v == m) {
+            const uint32_t k = b.meta & 0xffu;
+            const uint32_t jlo = (b.meta >> 8) & 0xffu;
+            const uint32_t jhi = (b.meta >> 16) & 0xffu;
+            float v[8];
+            load_level_sector(lv, k, b.s, pol, v);
+            uint32_t j = jlo;
+#pragma unroll
+            for (int jj = 7; jj >= 0; --jj)
+                if (uint32_t(jj) >= jlo && uint32_t(jj) < jhi && v[jj] == m) j = uint32_t(jj);
+            float val = v[0];
+#pragma unroll
+            for (int jj = 1; jj < 8; ++jj) val = (uint32_t(jj) == j) ? v[jj] : val;
+            const uint32_t e = b.s + j;
+            if (out_idx != nullptr) st_stream(out_idx + qi, k == 0 ? e : ld_index(lv.idx[k] + e));
+            if (out_min != nullptr) st_stream(out_min + qi, val);
         }
     }
 }
@@ -359,12 +594,13 @@ static cudaError_t launch_with_window(K kernel, uint32_t grid, const QueryArgs& 
 
 template <int R>
 static cudaError_t launch_query_r(const QueryArgs& a, cudaStream_t s) {
-    const uint32_t grid = (a.q + 255u) / 256u;
     const bool argmin = a.out_idx != nullptr;
     if (a.variant == 2) {
+        const uint32_t grid = (a.q + 255u) / 256u;
         return argmin ? launch_with_window(query_vl_kernel<R, true>, grid, a, s)
                       : launch_with_window(query_vl_kernel<R, false>, grid, a, s);
     }
+    const uint32_t grid = uint32_t((uint64_t(a.q) * uint64_t(a.lanes) + 255u) / 256u);
     switch (a.lanes) {
         case 4:
             return argmin ? launch_with_window(query_cl_kernel<R, 4, true>, grid, a, s)

@@ -16,12 +16,15 @@ Reference mapping (reference files, by path within the reference project):
 from __future__ import annotations
 
 import ctypes
+import os
 from pathlib import Path
 
 import numpy as np
 
 PKG = Path(__file__).resolve().parent
-LIB_PATH = PKG / "librmq_gb300.so"
+# RMQ_GB300_LIB overrides the library path (e.g. an alternative build of the
+# same sources); the default is the in-tree build.
+LIB_PATH = Path(os.environ.get("RMQ_GB300_LIB", str(PKG / "librmq_gb300.so")))
 GEN_PATH = PKG / "librmq_gen.so"
 
 RMQ_OK = 0

@@ -46,9 +46,9 @@ typedef enum {
 } rmq_status;
 
 typedef enum {
-    RMQ_VARIANT_AUTO = 0,  /* pick by array size / threshold (tuned table)            */
-    RMQ_VARIANT_CL = 1,    /* lane-group cooperative scans (reference alg 16 family)  */
-    RMQ_VARIANT_VL = 2     /* one thread per query, 256-bit loads (reference alg 20)  */
+    RMQ_VARIANT_AUTO = 0,  /* the measured best: VL with rf = 8                                          */
+    RMQ_VARIANT_CL = 1,    /* lane tile per query, lanes split the pieces by level (reference alg 16 family) */
+    RMQ_VARIANT_VL = 2     /* one thread per query, 256-bit loads (reference alg 20 family)              */
 } rmq_variant;
 
 typedef struct {
