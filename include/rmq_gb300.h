@@ -117,6 +117,29 @@ void rmq_destroy(rmq_handle* h);
 /* Static, human-readable name of a status code. */
 const char* rmq_strerror(int status);
 
+/* Range argmin (and, when d_min_or_null is not NULL, minima) of q inclusive
+ * queries over d_values[0..n), without any device allocation.  For callers
+ * that cannot allocate device memory when they query: hosts that reserve the
+ * whole device for their own memory pool, and latency-bound callers for whom
+ * cudaMalloc / cudaFree are off limits because those calls can block and
+ * synchronise the device.  It has no counterpart in the reference.
+ *
+ * The hierarchy (VL, rf = 8, scan threshold t; 0 = 32) is built into one
+ * fixed 8 MiB device array owned by the library, which every GPU that loads
+ * the library holds until the process exits; then the queries are answered,
+ * both on `stream`.  Limit: n <= 2^22 (4,194,304 entries); a larger n, or a t
+ * whose levels do not fit, returns RMQ_ERR_UNSUPPORTED before any device
+ * work.  The first call on each device looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * All calls on a device share the array, which keeps the last call's
+ * contents (each call rewrites every entry it reads, so nothing needs
+ * clearing): calls whose device work overlaps, on different streams or from
+ * different host threads, race on it.  Inputs and results are as for
+ * rmq_query_idx; d_values must be 32-byte aligned. */
+int rmq_query_idx_static(const float* d_values, uint64_t n, uint64_t scan_threshold,
+                         const uint32_t* d_lr, uint64_t q, uint32_t* d_argmin,
+                         float* d_min_or_null, rmq_stream_t stream);
+
 /* Level layout only (host computation, no device work): the reference's rule
  * (src/xxx.h:225-243) generalised to rf = 2^rf_log.  Returns RMQ_ERR_ARG when
  * t is below the variant's minimum.  Usable without a GPU. */
