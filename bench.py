@@ -453,12 +453,134 @@ def run_e2e(args, h, qs, dev, ws) -> dict:
             "d2h_bytes_per_step": 8 * q, "chunk_queries": chunk, "kernel_launches_per_step": nchunks}
 
 
+def run_batched(args, ws, rank, local):
+    """Batched workload: 4096 arrays, sizes log-uniform in [2^10, 2^22],
+    uniform [0, 1) values, min(4 x size, 2^20) queries per array with lengths
+    lognormal(median sqrt(size), sigma 1) clamped to [1, size].  One step =
+    build of every array + every query (one CUDA graph launch), inputs
+    resident.  Compared with per-array loops of the plain kernel."""
+    import torch
+    import rmq_gb300 as R
+    from oracle import oracle
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    dist_init(ws, "nccl")
+    rng = np.random.default_rng(args.seed + rank)
+    A = args.batch_arrays
+    sizes = np.exp(rng.uniform(np.log(2.0 ** 10), np.log(2.0 ** 22), A)).astype(np.uint64)
+    offs, total = R.pack_offsets(sizes)
+    qcounts = np.minimum(4 * sizes, np.uint64(1 << 20))
+    qo = np.zeros(A + 1, dtype=np.uint64)
+    qo[1:] = np.cumsum(qcounts)
+    Q = int(qo[-1])
+    values = torch.empty(total, dtype=torch.float32, device=dev)
+    R.gen_values_device(values, args.seed + 1000 * rank)
+    lr = torch.empty((Q, 2), dtype=torch.int32, device=dev)
+    for a in range(A):
+        s0, s1 = int(qo[a]), int(qo[a + 1])
+        R.gen_queries_device(lr[s0:s1], int(sizes[a]), 1, float(np.sqrt(float(sizes[a]))), 1.0,
+                             args.seed * 7919 + a)
+    out_min = torch.empty(Q, dtype=torch.float32, device=dev)
+    out_idx = torch.empty(Q, dtype=torch.int32, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.synchronize()
+
+    b = R.Batch(values, offs, sizes, t=64, stream=stream)
+    b.set_queries(lr, qo, out_idx, out_min, stream=stream)
+    tuned = b.autotune(stream=stream)
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            b.run(stream=stream)
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    barrier(ws)
+    with ClockSampler(local) as clocks:
+        ev[0].record(stream)
+        for _ in range(args.steps):
+            b.run(stream=stream)
+        ev[1].record(stream)
+        torch.cuda.synchronize()
+    total_ms = max_over_ranks(ev[0].elapsed_time(ev[1]), ws, dev)
+    value = aggregate_value(Q, args.steps, total_ms, ws)
+    # build-only and query-only timings (same kernels, outside the graph)
+    e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    e0.record(stream)
+    b.build(stream=stream)
+    e1.record(stream)
+    b.query(stream=stream)
+    e2.record(stream)
+    torch.cuda.synchronize()
+    build_ms, query_ms = e0.elapsed_time(e1), e1.elapsed_time(e2)
+
+    # parity: a seeded sample of arrays against the CPU oracle
+    parity = True
+    for a in rng.choice(A, size=min(A, 8), replace=False):
+        o, n = int(offs[a]), int(sizes[a])
+        s0, s1 = int(qo[a]), int(qo[a + 1])
+        x = values[o:o + n].cpu().numpy()
+        qh = lr[s0:s1].cpu().numpy().view(np.uint32)
+        parity &= out_min[s0:s1].cpu().numpy().tobytes() == oracle.rmq_min(x, qh).tobytes()
+        parity &= np.array_equal(out_idx[s0:s1].cpu().numpy().view(np.uint32), oracle.rmq_argmin(x, qh))
+
+    # per-array loops of the plain kernel (rmq_build + rmq_query_idx per array)
+    hs = []
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for a in range(A):
+        o, n = int(offs[a]), int(sizes[a])
+        h = R.Hierarchy(values[o:o + n], variant="vl", t=64, stream=stream)
+        s0, s1 = int(qo[a]), int(qo[a + 1])
+        h.query_idx_raw(int(lr[s0:s1].data_ptr()), s1 - s0, int(out_idx[s0:s1].data_ptr()),
+                        int(out_min[s0:s1].data_ptr()), stream)
+        hs.append(h)
+    torch.cuda.synchronize()
+    loop_api_s = time.perf_counter() - t0
+    e0.record(stream)
+    for a in range(A):
+        s0, s1 = int(qo[a]), int(qo[a + 1])
+        hs[a].query_idx_raw(int(lr[s0:s1].data_ptr()), s1 - s0, int(out_idx[s0:s1].data_ptr()),
+                            int(out_min[s0:s1].data_ptr()), stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    loop_query_ms = e0.elapsed_time(e1)
+    for h in hs:
+        h.close()
+    b.close()
+
+    line = {
+        "metric": "RMQ queries/s (batched: build + queries of every array per step)", "value": value,
+        "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (device counter-based generators)",
+        "config": {"workload": f"batched: {A} arrays, sizes log-uniform [2^10, 2^22], "
+                               "queries min(4 size, 2^20) lognormal(sqrt(size), 1.0); min + argmin",
+                   "arrays": A, "total_values": total, "total_queries": Q, "seed": args.seed,
+                   "l2": "inputs larger than L2 (no flush)"},
+        "autotuned": {"scan_threshold": int(tuned.scan_threshold), "query_block": int(tuned.query_block),
+                      "query_ms": float(tuned.query_ms)},
+        "build_ms": build_ms, "query_ms": query_ms,
+        "loop_public_api": {"value": Q / loop_api_s, "seconds": loop_api_s,
+                            "what": "per array: rmq_build (alloc + build + sync) + rmq_query_idx"},
+        "loop_prebuilt_queries": {"value": Q / (loop_query_ms / 1e3), "ms": loop_query_ms,
+                                  "what": "per array: rmq_query_idx launch on a prebuilt handle"},
+        "speedup_vs_loop_public_api": value / (Q / loop_api_s),
+        "speedup_vs_loop_prebuilt_queries": (Q / (query_ms / 1e3)) / (Q / (loop_query_ms / 1e3)),
+        "clocks": clocks.summary(), "gpu_launches": 3 * args.steps, "parity_sample_ok": bool(parity),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def parse_args(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--mode", choices=["plain", "batched"], default="plain",
+                    help="plain = the single-array workload (default); batched = 4096 arrays")
+    ap.add_argument("--batch-arrays", dest="batch_arrays", type=int, default=4096)
     ap.add_argument("--n", type=int, default=1 << 26)
     ap.add_argument("--q", type=int, default=1 << 26)
     ap.add_argument("--lr", type=int, default=-7, help="length law code (-7 = lognormal median 2^13 sigma 1)")
@@ -482,6 +604,9 @@ def main(argv=None):
     ws, rank, local = dist_env()
     if args.impl == "reference":
         run_reference(args, ws, rank)
+        return
+    if args.mode == "batched":
+        run_batched(args, ws, rank, local)
         return
     run_ours(args, ws, rank, local)
 

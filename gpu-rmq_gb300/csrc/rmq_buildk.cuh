@@ -1,0 +1,133 @@
+// rmq_buildk.cuh — build device functions shared by the single-array build
+// (rmq_build.cu) and the batched build (rmq_batch.cu).
+#pragma once
+
+#include "rmq_common.cuh"
+
+namespace rmq {
+
+constexpr uint32_t kTile = 8192;
+constexpr uint32_t kTileSectors = kTile / 8;
+constexpr uint32_t kFusedThreads = 256;
+constexpr uint32_t kTailMaxEntries = 16384;  // largest level the tail CTA reads
+
+struct LevelOut {
+    float* val[kMaxLevels];
+    uint32_t* idx[kMaxLevels];  // null entries when argmin arrays are not built
+    uint32_t size[kMaxLevels];
+};
+
+// First-occurrence minimum over candidates visited in ascending position;
+// p == kNoPos marks an absent candidate.
+struct VP {
+    float v;
+    uint32_t p;
+};
+
+__device__ __forceinline__ void vp_take(VP& cur, float v, uint32_t p) {
+    if (p != kNoPos && (cur.p == kNoPos || v < cur.v)) {
+        cur.v = v;
+        cur.p = p;
+    }
+}
+
+template <int R>
+__host__ __device__ constexpr uint32_t fused_depth() {
+    return 13u / uint32_t(R);  // largest m with rf^m <= kTile = 2^13
+}
+
+// One CTA of kFusedThreads threads builds levels 1..depth of `tile` (entries
+// [tile * kTile, (tile + 1) * kTile) of level 0); sv / sp are kTileSectors
+// entries of shared memory.
+template <int R>
+__device__ __forceinline__ void fused_tile(const float* __restrict__ a, uint32_t n, const LevelOut& out,
+                                           uint32_t depth, uint32_t tile, float* sv, uint32_t* sp) {
+    constexpr uint32_t RF = 1u << R;
+    constexpr uint32_t SPB = RF / 8u;  // sectors per level-1 block
+    const uint32_t tid = threadIdx.x;
+    const uint64_t base = uint64_t(tile) * kTile;
+    const uint64_t pol = policy_evict_first();
+
+    // Stage 0: per-sector first minimum.
+#pragma unroll
+    for (uint32_t i = 0; i < kTileSectors / kFusedThreads; ++i) {
+        const uint32_t sec = tid + kFusedThreads * i;
+        const uint64_t s = base + 8u * sec;
+        VP c{f_inf(), kNoPos};
+        if (s < n) {
+            float v[8];
+            if (s + 8u <= n) {
+                ld_sector_policy(a + s, v, pol);
+            } else {
+#pragma unroll
+                for (int j = 0; j < 8; ++j) v[j] = (s + j < n) ? a[s + j] : f_inf();
+            }
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+                if (s + j < n) vp_take(c, v[j], uint32_t(s + j));
+        }
+        sv[sec] = c.v;
+        sp[sec] = c.p;
+    }
+    __syncthreads();
+
+    // Levels 1..depth: level k has kTile / rf^k entries in the tile; an entry
+    // combines rf children of level k-1 (SPB sectors for k = 1).
+    uint32_t children = kTileSectors;  // entries of the previous stage held in smem
+    for (uint32_t k = 1; k <= depth; ++k) {
+        const uint32_t fan = (k == 1) ? SPB : RF;
+        const uint32_t cnt = children / fan;
+        constexpr uint32_t kMaxPer = kTileSectors / kFusedThreads;  // <= 4 entries per thread
+        VP res[kMaxPer];
+#pragma unroll
+        for (uint32_t i = 0; i < kMaxPer; ++i) {
+            const uint32_t e = tid + kFusedThreads * i;
+            res[i] = VP{f_inf(), kNoPos};
+            if (e < cnt) {
+                for (uint32_t j = 0; j < fan; ++j) vp_take(res[i], sv[e * fan + j], sp[e * fan + j]);
+            }
+        }
+        __syncthreads();
+        const uint64_t gbase = uint64_t(tile) * cnt;
+#pragma unroll
+        for (uint32_t i = 0; i < kMaxPer; ++i) {
+            const uint32_t e = tid + kFusedThreads * i;
+            if (e < cnt) {
+                sv[e] = res[i].v;
+                sp[e] = res[i].p;
+                const uint64_t g = gbase + e;
+                if (g < out.size[k]) {
+                    out.val[k][g] = res[i].v;
+                    if (out.idx[k] != nullptr) out.idx[k][g] = res[i].p;
+                }
+            }
+        }
+        __syncthreads();
+        children = cnt;
+    }
+}
+
+// Single CTA: builds levels from+1 .. last from level `from` (already built),
+// level after level, with a block barrier between levels (global writes of
+// the block are visible to it after __syncthreads).
+template <int R>
+__device__ __forceinline__ void tail_levels(const LevelOut& out, uint32_t from, uint32_t last) {
+    constexpr uint32_t RF = 1u << R;
+    for (uint32_t k = from; k < last; ++k) {
+        const float* src = out.val[k];
+        const uint32_t* src_idx = out.idx[k];
+        const uint32_t src_size = out.size[k];
+        for (uint32_t e = threadIdx.x; e < out.size[k + 1]; e += blockDim.x) {
+            VP c{f_inf(), kNoPos};
+            for (uint32_t j = 0; j < RF; ++j) {
+                const uint32_t ch = e * RF + j;
+                if (ch < src_size) vp_take(c, src[ch], src_idx != nullptr ? src_idx[ch] : ch);
+            }
+            out.val[k + 1][e] = c.v;
+            if (out.idx[k + 1] != nullptr) out.idx[k + 1][e] = c.p;
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace rmq

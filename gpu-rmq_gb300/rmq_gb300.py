@@ -300,3 +300,147 @@ def sample_indices(original_size: int, sample_size: int, seed: int) -> np.ndarra
     out = np.empty(min(original_size, sample_size), dtype=np.uint32)
     m = genlib().rmq_gen_sample_indices(original_size, sample_size, seed, out.ctypes.data)
     return out[:m]
+
+
+# ---- batched queries over many arrays (include/rmq_gb300_batch.h) ------------
+
+class BatchInfo(ctypes.Structure):
+    _fields_ = [
+        ("num_arrays", ctypes.c_uint32),
+        ("total_values", ctypes.c_uint64),
+        ("level_bytes", ctypes.c_uint64),
+        ("scan_threshold", ctypes.c_uint64),
+        ("query_block", ctypes.c_uint32),
+        ("max_levels", ctypes.c_uint32),
+        ("total_queries", ctypes.c_uint64),
+        ("build_ms", ctypes.c_float),
+        ("query_ms", ctypes.c_float),
+    ]
+
+
+_batch_bound = False
+
+
+def _bind_batch() -> ctypes.CDLL:
+    global _batch_bound
+    L = lib()
+    if not _batch_bound:
+        L.rmq_batch_create.argtypes = [_P, _P, _P, ctypes.c_uint32, ctypes.POINTER(RMQConfig), _P,
+                                       ctypes.POINTER(_P)]
+        L.rmq_batch_set_queries.argtypes = [_P, _P, _P, _P, _P, _P]
+        for name in ("rmq_batch_build", "rmq_batch_query", "rmq_batch_run"):
+            getattr(L, name).argtypes = [_P, _P]
+        L.rmq_batch_autotune.argtypes = [_P, _P, ctypes.POINTER(BatchInfo)]
+        L.rmq_batch_get_info.argtypes = [_P, ctypes.POINTER(BatchInfo)]
+        L.rmq_batch_destroy.argtypes = [_P]
+        L.rmq_batch_destroy.restype = None
+        L.rmq_gen_values_device.argtypes = [_P, _U64, _U64, _P]
+        L.rmq_gen_queries_device.argtypes = [_P, _U64, _U64, ctypes.c_int32, ctypes.c_double,
+                                             ctypes.c_double, _U64, _P]
+        _batch_bound = True
+    return L
+
+
+class Batch:
+    """Many independent arrays packed in one device tensor; one build pass and
+    one query launch (or one graph launch) for all of them."""
+
+    def __init__(self, values, value_offsets, sizes, t: int = 0, with_index: bool = True, stream=None):
+        L = _bind_batch()
+        self.values = values
+        self.offsets = np.ascontiguousarray(value_offsets, dtype=np.uint64)
+        self.sizes = np.ascontiguousarray(sizes, dtype=np.uint64)
+        self.num_arrays = int(self.sizes.size)
+        cfg = config("vl", t, 3, 0, with_index)
+        h = _P()
+        st = L.rmq_batch_create(_dev_ptr(values), self.offsets.ctypes.data, self.sizes.ctypes.data,
+                                self.num_arrays, ctypes.byref(cfg), _stream_handle(stream), ctypes.byref(h))
+        if st != RMQ_OK:
+            raise RMQError(st, "rmq_batch_create")
+        self._h = h
+        self._keep = ()
+
+    def set_queries(self, lr, query_offsets, out_idx=None, out_min=None, stream=None):
+        qo = np.ascontiguousarray(query_offsets, dtype=np.uint64)
+        self._keep = (lr, out_idx, out_min, qo)
+        st = _bind_batch().rmq_batch_set_queries(
+            self._h, _dev_ptr(lr) if lr.numel() else None, qo.ctypes.data,
+            _dev_ptr(out_idx) if out_idx is not None else None,
+            _dev_ptr(out_min) if out_min is not None else None, _stream_handle(stream))
+        if st != RMQ_OK:
+            raise RMQError(st, "rmq_batch_set_queries")
+
+    def _call(self, name, stream):
+        st = getattr(_bind_batch(), name)(self._h, _stream_handle(stream))
+        if st != RMQ_OK:
+            raise RMQError(st, name)
+
+    def build(self, stream=None):
+        self._call("rmq_batch_build", stream)
+
+    def query(self, stream=None):
+        self._call("rmq_batch_query", stream)
+
+    def run(self, stream=None):
+        self._call("rmq_batch_run", stream)
+
+    def autotune(self, stream=None) -> BatchInfo:
+        info = BatchInfo()
+        st = _bind_batch().rmq_batch_autotune(self._h, _stream_handle(stream), ctypes.byref(info))
+        if st != RMQ_OK:
+            raise RMQError(st, "rmq_batch_autotune")
+        return info
+
+    def info(self) -> BatchInfo:
+        info = BatchInfo()
+        st = _bind_batch().rmq_batch_get_info(self._h, ctypes.byref(info))
+        if st != RMQ_OK:
+            raise RMQError(st, "rmq_batch_get_info")
+        return info
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            _bind_batch().rmq_batch_destroy(self._h)
+            self._h = _P()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+def gen_values_device(out, seed: int, stream=None):
+    """Fills a CUDA float32 tensor with seeded uniform [0, 1) values."""
+    st = _bind_batch().rmq_gen_values_device(_dev_ptr(out), out.numel(), seed, _stream_handle(stream))
+    if st != RMQ_OK:
+        raise RMQError(st, "rmq_gen_values_device")
+    return out
+
+
+def gen_queries_device(out, n: int, law: int, median: float = 1.0, sigma: float = 0.0, seed: int = 0,
+                       stream=None):
+    """Fills a CUDA int32 tensor of shape [q, 2] with seeded inclusive queries
+    over n entries (law 0 = uniform length, 1 = lognormal(median, sigma))."""
+    st = _bind_batch().rmq_gen_queries_device(_dev_ptr(out), out.numel() // 2, n, law, median, sigma, seed,
+                                              _stream_handle(stream))
+    if st != RMQ_OK:
+        raise RMQError(st, "rmq_gen_queries_device")
+    return out
+
+
+def pack_offsets(sizes, align: int = 8) -> tuple[np.ndarray, int]:
+    """Packed offsets of arrays laid end to end, each start a multiple of
+    `align` entries (32 bytes for fp32 at align = 8); returns (offsets, total)."""
+    sizes = np.asarray(sizes, dtype=np.uint64)
+    padded = (sizes + np.uint64(align - 1)) // np.uint64(align) * np.uint64(align)
+    offs = np.zeros(sizes.size, dtype=np.uint64)
+    if sizes.size > 1:
+        offs[1:] = np.cumsum(padded)[:-1]
+    return offs, int(padded.sum())
