@@ -572,14 +572,164 @@ def run_batched(args, ws, rank, local):
         print(json.dumps(line), flush=True)
 
 
+def serve_trace(rng, sizes, seconds, rate, reg_frac, seed):
+    """Poisson request stream: arrivals at `rate`/s for `seconds`; a fraction
+    reg_frac registers a new array (size law of the resident ones), the rest
+    are requests naming a registered array, with 1..2^16 queries (log-uniform)
+    of lognormal(2^13, 1) lengths clamped to the array."""
+    import rmq_gb300 as R
+    gaps = rng.exponential(1.0 / rate, int(seconds * rate * 1.5) + 16)
+    t = np.cumsum(gaps)
+    t = t[t < seconds]
+    E = t.size
+    ev = np.zeros(E, dtype=R.TRACE_DTYPE)
+    ev["t_arrival_s"] = t
+    n_of = list(sizes)
+    is_reg = rng.random(E) < reg_frac
+    qcount = np.exp(rng.uniform(0.0, np.log(2.0 ** 16), E)).astype(np.int64).clip(1, 1 << 16)
+    off = 0
+    req_n = np.zeros(E, dtype=np.int64)
+    for i in range(E):
+        if is_reg[i]:
+            n = int(np.exp(rng.uniform(np.log(2.0 ** 16), np.log(2.0 ** 26))))
+            ev["kind"][i] = 1
+            ev["n"][i] = n
+            ev["seed"][i] = seed * 1000003 + len(n_of)
+            n_of.append(n)
+        else:
+            aid = int(rng.integers(0, len(n_of)))
+            ev["array_id"][i] = aid
+            ev["q_offset"][i] = off
+            ev["q"][i] = qcount[i]
+            req_n[i] = n_of[aid]
+            off += int(qcount[i])
+    lr = np.empty((off, 2), dtype=np.uint32)
+    for i in np.flatnonzero(~is_reg):
+        q, n, o = int(ev["q"][i]), int(req_n[i]), int(ev["q_offset"][i])
+        length = np.rint(np.exp(rng.normal(np.log(8192.0), 1.0, q))).clip(1, n).astype(np.int64)
+        l = (rng.random(q) * (n - length + 1)).astype(np.int64)
+        lr[o:o + q, 0] = l
+        lr[o:o + q, 1] = l + length - 1
+    return ev, lr, n_of
+
+
+def run_serve(args, ws, rank, local):
+    """Serving workload: 256 resident arrays (sizes log-uniform [2^16, 2^26],
+    device-generated values), a Poisson stream of 20k requests/s for
+    --serve-seconds, 5 % of them registering a new array, 64 GiB HBM budget
+    with LRU eviction; p50/p99 request latency and queries/s, plus the same
+    requests issued at once (capacity) against a per-request loop of the
+    plain kernel through the public API."""
+    import torch
+    import rmq_gb300 as R
+    from oracle import oracle
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    rng = np.random.default_rng(args.seed + rank)
+    sizes = [int(np.exp(rng.uniform(np.log(2.0 ** 16), np.log(2.0 ** 26)))) for _ in range(256)]
+    seed_of = lambda a: args.seed * 1000003 + a  # noqa: E731  (the trace uses the same rule)
+    ev, lr, n_of = serve_trace(rng, sizes, args.serve_seconds, 20000.0, 0.05, args.seed)
+    req = ev["kind"] == 0
+    Q = int(ev["q"][req].sum())
+    out_i = np.empty(Q, dtype=np.uint32)
+    out_m = np.empty(Q, dtype=np.float32)
+
+    srv = R.Server(hbm_budget_bytes=64 << 30, slots=args.serve_slots, t=64)
+    for a, n in enumerate(sizes):
+        srv.register_generated(n, seed_of(a))
+    warm = np.zeros((1, 2), dtype=np.uint32)
+    wi, wm = np.empty(1, np.uint32), np.empty(1, np.float32)
+    for a in range(len(sizes)):
+        srv.wait(srv.submit(a, warm, wi, wm))  # every initial array built
+    with ClockSampler(local) as clocks:
+        lat, wall = srv.replay(ev, lr, out_i, out_m)
+    st = srv.stats()
+    lat_req = lat[req & (lat >= 0)]
+
+    # parity: a sample of requests on the smaller arrays against the CPU oracle
+    parity = True
+    cand = [i for i in np.flatnonzero(req) if n_of[int(ev["array_id"][i])] <= (1 << 22)]
+    for i in rng.choice(cand, size=min(len(cand), 6), replace=False):
+        aid, o, q = int(ev["array_id"][i]), int(ev["q_offset"][i]), int(ev["q"][i])
+        v = torch.empty(n_of[aid], dtype=torch.float32, device=dev)
+        R.gen_values_device(v, seed_of(aid))
+        x = v.cpu().numpy()
+        parity &= np.array_equal(out_i[o:o + q], oracle.rmq_argmin(x, lr[o:o + q]))
+        parity &= out_m[o:o + q].tobytes() == oracle.rmq_min(x, lr[o:o + q]).tobytes()
+
+    # capacity: requests on the initial arrays, all issued at once
+    cap_ev = ev[req & (ev["array_id"] < len(sizes))].copy()
+    cap_ev["t_arrival_s"] = 0.0
+    cap_q = int(cap_ev["q"].sum())
+    _, cap_wall = srv.replay(cap_ev, lr, out_i, out_m)
+    srv.close()
+
+    # per-request loop of the plain kernel through the public API (pinned host
+    # buffers, copy in, rmq_query_idx, copy out, synchronise)
+    vals, hs = [], []
+    stream = torch.cuda.Stream(device=dev)
+    for a, n in enumerate(sizes):
+        v = torch.empty(n, dtype=torch.float32, device=dev)
+        R.gen_values_device(v, seed_of(a))
+        vals.append(v)
+        hs.append(R.Hierarchy(v, variant="vl", t=64, stream=stream))
+    h_lr = torch.from_numpy(lr.view(np.int32).reshape(-1)).pin_memory()
+    h_i = torch.empty(Q, dtype=torch.int32).pin_memory()
+    h_m = torch.empty(Q, dtype=torch.float32).pin_memory()
+    qmax = int(cap_ev["q"].max())
+    d_lr = torch.empty(2 * qmax, dtype=torch.int32, device=dev)
+    d_i = torch.empty(qmax, dtype=torch.int32, device=dev)
+    d_m = torch.empty(qmax, dtype=torch.float32, device=dev)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    with torch.cuda.stream(stream):
+        for e in cap_ev:
+            o, q, aid = int(e["q_offset"]), int(e["q"]), int(e["array_id"])
+            d_lr[: 2 * q].copy_(h_lr[2 * o: 2 * (o + q)], non_blocking=True)
+            hs[aid].query_idx_raw(int(d_lr.data_ptr()), q, int(d_i.data_ptr()), int(d_m.data_ptr()), stream)
+            h_i[o:o + q].copy_(d_i[:q], non_blocking=True)
+            h_m[o:o + q].copy_(d_m[:q], non_blocking=True)
+            stream.synchronize()
+    loop_s = time.perf_counter() - t0
+    for h in hs:
+        h.close()
+
+    line = {
+        "metric": "RMQ queries/s (served: continuous batching)", "value": Q / wall, "unit": UNIT,
+        "n_gpus": ws, "steps": 1, "warmup": 1, "ms_per_step": wall * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Poisson trace)",
+        "config": {"workload": "serving: 256 resident arrays log-uniform [2^16, 2^26], Poisson 20k req/s, "
+                               "1..2^16 queries per request (log-uniform), lognormal(2^13, 1) lengths, "
+                               "5 % registrations, 64 GiB budget, LRU eviction",
+                   "seconds": args.serve_seconds, "events": int(ev.size), "requests": int(req.sum()),
+                   "queries": Q, "slots": args.serve_slots, "seed": args.seed},
+        "latency_us": {"p50": float(np.percentile(lat_req, 50)), "p99": float(np.percentile(lat_req, 99)),
+                       "mean": float(lat_req.mean()), "max": float(lat_req.max())},
+        "offered_queries_per_s": Q / float(ev["t_arrival_s"][-1]),
+        "server_stats": st,
+        "capacity": {"value": cap_q / cap_wall, "requests": int(cap_ev.size), "queries": cap_q,
+                     "what": "same requests on the initial arrays, all arriving at once"},
+        "loop_public_api": {"value": cap_q / loop_s, "seconds": loop_s,
+                            "what": "per request: H2D queries, rmq_query_idx, D2H results, sync (Python loop)"},
+        "speedup_capacity_vs_loop": (cap_q / cap_wall) / (cap_q / loop_s),
+        "clocks": clocks.summary(), "parity_sample_ok": bool(parity),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def parse_args(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--mode", choices=["plain", "batched"], default="plain",
-                    help="plain = the single-array workload (default); batched = 4096 arrays")
+    ap.add_argument("--mode", choices=["plain", "batched", "serve"], default="plain",
+                    help="plain = the single-array workload (default); batched = 4096 arrays; "
+                         "serve = the request-serving loop")
+    ap.add_argument("--serve-seconds", dest="serve_seconds", type=float, default=2.0)
+    ap.add_argument("--serve-slots", dest="serve_slots", type=int, default=4)
     ap.add_argument("--batch-arrays", dest="batch_arrays", type=int, default=4096)
     ap.add_argument("--n", type=int, default=1 << 26)
     ap.add_argument("--q", type=int, default=1 << 26)
@@ -607,6 +757,9 @@ def main(argv=None):
         return
     if args.mode == "batched":
         run_batched(args, ws, rank, local)
+        return
+    if args.mode == "serve":
+        run_serve(args, ws, rank, local)
         return
     run_ours(args, ws, rank, local)
 

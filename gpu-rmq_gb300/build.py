@@ -31,7 +31,7 @@ BUILD = PKG / "_build" / platform.machine()
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 CUDA_SOURCES = ["rmq_build.cu", "rmq_query.cu", "rmq_api.cu", "rmq_noalloc.cu", "rmq_batch.cu",
-                "rmq_gen_device.cu"]
+                "rmq_gen_device.cu", "rmq_serve.cu"]
 
 LIB = PKG / "librmq_gb300.so"
 GENLIB = PKG / "librmq_gen.so"

@@ -22,14 +22,6 @@
 
 namespace rmq {
 
-struct ArrayDesc {
-    uint64_t val_off;   // first value of the array in the caller's buffer
-    uint64_t lvl_base;  // first entry of the array's levels in the level buffers
-    uint32_t num_levels;
-    uint32_t size[kMaxLevels];
-    uint32_t off[kMaxLevels];  // level k >= 1 starts at lvl_base + off[k]
-};
-
 // Largest a in [0, num) with offs[a] <= x, for non-decreasing offs with
 // offs[0] = 0 <= x < offs[num]; arrays owning no work are skipped.
 __device__ __forceinline__ uint32_t find_owner(const uint64_t* __restrict__ offs, uint32_t num, uint64_t x) {
@@ -46,7 +38,7 @@ __device__ __forceinline__ void fill_levelout(const ArrayDesc& d, float* lvl_val
     for (uint32_t k = 0; k < uint32_t(kMaxLevels); ++k) {
         const bool has = k > 0 && k < d.num_levels;
         lo.val[k] = has ? lvl_val + d.lvl_base + d.off[k] : nullptr;
-        lo.idx[k] = (has && lvl_idx != nullptr) ? lvl_idx + d.lvl_base + d.off[k] : nullptr;
+        lo.idx[k] = (has && lvl_idx != nullptr) ? lvl_idx + d.idx_base + d.off[k] : nullptr;
         lo.size[k] = k < d.num_levels ? d.size[k] : 0u;
     }
 }
@@ -125,7 +117,7 @@ batch_query_kernel(const float* __restrict__ values, const ArrayDesc* __restrict
         const uint32_t k = lane;
         const bool has = k > 0 && k < nl;
         lv.val[k] = k == 0 ? values + d.val_off : (has ? lvl_val + d.lvl_base + d.off[k] : nullptr);
-        lv.idx[k] = (has && lvl_idx != nullptr) ? lvl_idx + d.lvl_base + d.off[k] : nullptr;
+        lv.idx[k] = (has && lvl_idx != nullptr) ? lvl_idx + d.idx_base + d.off[k] : nullptr;
         lv.size[k] = k < nl ? d.size[k] : 0u;
     } else if (lane == 31) {
         lv.num_levels = nl;
@@ -146,6 +138,28 @@ batch_query_kernel(const float* __restrict__ values, const ArrayDesc* __restrict
     const uint64_t at = wq[warp][0] + lane;  // base re-read after the descent
     vl_store<ARGMIN>(in_range, valid, v, idx, out_min != nullptr ? out_min + at : nullptr,
                      ARGMIN ? out_idx + at : nullptr, nullptr);
+}
+
+cudaError_t launch_fill_owner(const uint64_t* unit_off, uint32_t num, uint32_t* owner, cudaStream_t s) {
+    if (num == 0) return cudaSuccess;
+    fill_owner_kernel<<<num, 256, 0, s>>>(unit_off, owner);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_query(const BatchQueryArgs& a, cudaStream_t s) {
+    if (a.total_units == 0) return cudaSuccess;
+    const uint32_t warps = a.threads / 32u;
+    const uint32_t grid = uint32_t((a.total_units + warps - 1) / warps);
+    if (a.out_idx != nullptr) {
+        batch_query_kernel<3, true><<<grid, a.threads, 0, s>>>(a.values, a.descs, a.owner, a.unit_off, a.q_off,
+                                                               a.total_units, a.lvl_val, a.lvl_idx, a.qs,
+                                                               a.out_min, a.out_idx);
+    } else {
+        batch_query_kernel<3, false><<<grid, a.threads, 0, s>>>(a.values, a.descs, a.owner, a.unit_off, a.q_off,
+                                                                a.total_units, a.lvl_val, a.lvl_idx, a.qs,
+                                                                a.out_min, nullptr);
+    }
+    return cudaGetLastError();
 }
 
 }  // namespace rmq
@@ -224,6 +238,7 @@ int plan(rmq_batch* b, uint64_t t, cudaStream_t s) {
         std::memset(&d, 0, sizeof(d));
         d.val_off = b->val_off[a];
         d.lvl_base = base;
+        d.idx_base = base;
         d.num_levels = lay.num_levels;
         for (uint32_t k = 0; k < lay.num_levels; ++k) {
             d.size[k] = uint32_t(lay.size[k]);
@@ -268,10 +283,7 @@ int upload_blocks(rmq_batch* b, cudaStream_t s) {
     }
     e = cudaMemcpyAsync(b->d_blk_off, blk.data(), sizeof(uint64_t) * (b->num_arrays + 1),
                         cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess && units > 0) {
-        rmq::fill_owner_kernel<<<b->num_arrays, 256, 0, s>>>(b->d_blk_off, b->d_owner);
-        e = cudaGetLastError();
-    }
+    if (e == cudaSuccess && units > 0) e = rmq::launch_fill_owner(b->d_blk_off, b->num_arrays, b->d_owner, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return status_of(e);
     b->total_blocks = units;
@@ -293,20 +305,20 @@ cudaError_t enqueue_build(rmq_batch* b, cudaStream_t s) {
 }
 
 cudaError_t enqueue_query(rmq_batch* b, cudaStream_t s) {
-    if (b->total_blocks == 0) return cudaSuccess;
-    const uint2* qs = reinterpret_cast<const uint2*>(b->d_lr);
-    const uint32_t warps = b->qblock / 32u;
-    const uint32_t grid = uint32_t((b->total_blocks + warps - 1) / warps);
-    if (b->d_argmin != nullptr) {
-        rmq::batch_query_kernel<3, true><<<grid, b->qblock, 0, s>>>(
-            b->d_values, b->d_descs, b->d_owner, b->d_blk_off, b->d_q_off, b->total_blocks, b->lvl_val,
-            b->lvl_idx, qs, b->d_min, b->d_argmin);
-    } else {
-        rmq::batch_query_kernel<3, false><<<grid, b->qblock, 0, s>>>(
-            b->d_values, b->d_descs, b->d_owner, b->d_blk_off, b->d_q_off, b->total_blocks, b->lvl_val,
-            b->lvl_idx, qs, b->d_min, nullptr);
-    }
-    return cudaGetLastError();
+    rmq::BatchQueryArgs a;
+    a.values = b->d_values;
+    a.descs = b->d_descs;
+    a.owner = b->d_owner;
+    a.unit_off = b->d_blk_off;
+    a.q_off = b->d_q_off;
+    a.total_units = b->total_blocks;
+    a.lvl_val = b->lvl_val;
+    a.lvl_idx = b->lvl_idx;
+    a.qs = reinterpret_cast<const uint2*>(b->d_lr);
+    a.out_min = b->d_min;
+    a.out_idx = b->d_argmin;
+    a.threads = b->qblock;
+    return rmq::launch_batch_query(a, s);
 }
 
 struct DeviceGuard {

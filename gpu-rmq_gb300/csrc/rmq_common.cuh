@@ -28,6 +28,16 @@ struct Layout {
     uint64_t total = 0;                // entries in the level buffer incl. alignment padding
 };
 
+// Descriptor of one array inside packed buffers (batched and served modes).
+struct ArrayDesc {
+    uint64_t val_off;   // first value of the array, in floats from the values base
+    uint64_t lvl_base;  // first entry of its coarse levels, from the level-value base
+    uint64_t idx_base;  // first entry of its argmin arrays, from the argmin base
+    uint32_t num_levels;
+    uint32_t size[kMaxLevels];
+    uint32_t off[kMaxLevels];  // level k >= 1 starts at lvl_base + off[k]
+};
+
 // Device-side view passed by value to the kernels (fits easily in the 32 KB
 // parameter space).
 struct Levels {

@@ -37,6 +37,27 @@ cudaError_t launch_query(const QueryArgs& a, cudaStream_t s);
 cudaError_t launch_bruteforce(const float* vals, uint32_t n, const uint2* qs, uint32_t q,
                               float* out_min, uint32_t* out_idx, cudaStream_t s);
 
+// Query launch over packed work: entry e (an array, or a request's array in
+// serving mode) owns queries [q_off[e], q_off[e+1]) of qs, in units of 32
+// queries per warp; owner[u] gives the entry of unit u (launch_fill_owner).
+struct BatchQueryArgs {
+    const float* values;
+    const ArrayDesc* descs;
+    const uint32_t* owner;
+    const uint64_t* unit_off;
+    const uint64_t* q_off;
+    uint64_t total_units;
+    const float* lvl_val;
+    const uint32_t* lvl_idx;
+    const uint2* qs;
+    float* out_min;
+    uint32_t* out_idx;  // null: minima only
+    uint32_t threads;   // CTA size, multiple of 32, <= 512
+};
+
+cudaError_t launch_batch_query(const BatchQueryArgs& a, cudaStream_t s);
+cudaError_t launch_fill_owner(const uint64_t* unit_off, uint32_t num, uint32_t* owner, cudaStream_t s);
+
 // Number of kernel launches the last launch_build issued (for accounting).
 int build_launch_count(const Layout& lay);
 

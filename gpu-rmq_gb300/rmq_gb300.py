@@ -444,3 +444,151 @@ def pack_offsets(sizes, align: int = 8) -> tuple[np.ndarray, int]:
     if sizes.size > 1:
         offs[1:] = np.cumsum(padded)[:-1]
     return offs, int(padded.sum())
+
+
+# ---- the query server (include/rmq_gb300_serve.h) ----------------------------
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [
+        ("hbm_budget_bytes", ctypes.c_uint64),
+        ("slots", ctypes.c_uint32),
+        ("max_batch_queries", ctypes.c_uint64),
+        ("max_batch_requests", ctypes.c_uint32),
+        ("scan_threshold", ctypes.c_uint64),
+        ("query_threads", ctypes.c_uint32),
+    ]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [(name, ctypes.c_uint64) for name in (
+        "requests_done", "queries_done", "batches", "registrations", "evictions", "readmissions",
+        "resident_arrays", "resident_bytes", "max_requests_per_batch", "max_batches_in_flight")]
+
+    def as_dict(self) -> dict:
+        return {name: int(getattr(self, name)) for name, _ in self._fields_}
+
+
+# rmq_trace_event as a numpy record (C layout: double, int32 + 4 padding, 5 x uint64)
+TRACE_DTYPE = np.dtype([("t_arrival_s", "<f8"), ("kind", "<i4"), ("_pad", "<i4"), ("array_id", "<u8"),
+                        ("n", "<u8"), ("seed", "<u8"), ("q_offset", "<u8"), ("q", "<u8")])
+
+_server_bound = False
+
+
+def _bind_server() -> ctypes.CDLL:
+    global _server_bound
+    L = lib()
+    if not _server_bound:
+        L.rmq_server_config_init.argtypes = [ctypes.POINTER(ServerConfig)]
+        L.rmq_server_config_init.restype = None
+        L.rmq_server_create.argtypes = [ctypes.POINTER(ServerConfig), ctypes.POINTER(_P)]
+        L.rmq_server_register_generated.argtypes = [_P, _U64, _U64, ctypes.POINTER(_U64)]
+        L.rmq_server_register_host.argtypes = [_P, _P, _U64, ctypes.POINTER(_U64)]
+        L.rmq_server_submit.argtypes = [_P, _U64, _P, _U64, _P, _P, ctypes.POINTER(_U64)]
+        L.rmq_server_wait.argtypes = [_P, _U64, ctypes.c_int64, ctypes.POINTER(ctypes.c_double)]
+        L.rmq_server_drain.argtypes = [_P, ctypes.c_int64]
+        L.rmq_server_replay.argtypes = [_P, _P, _U64, _P, _P, _P, _P, ctypes.POINTER(ctypes.c_double)]
+        L.rmq_server_get_stats.argtypes = [_P, ctypes.POINTER(ServerStats)]
+        L.rmq_server_destroy.argtypes = [_P]
+        L.rmq_server_destroy.restype = None
+        _server_bound = True
+    return L
+
+
+class Server:
+    """Resident-array RMQ server with continuous batching (host buffers in/out)."""
+
+    def __init__(self, hbm_budget_bytes: int = 0, slots: int = 0, max_batch_queries: int = 0,
+                 max_batch_requests: int = 0, t: int = 0, query_threads: int = 0):
+        L = _bind_server()
+        cfg = ServerConfig()
+        L.rmq_server_config_init(ctypes.byref(cfg))
+        for name, val in (("hbm_budget_bytes", hbm_budget_bytes), ("slots", slots),
+                          ("max_batch_queries", max_batch_queries), ("max_batch_requests", max_batch_requests),
+                          ("scan_threshold", t), ("query_threads", query_threads)):
+            if val:
+                setattr(cfg, name, val)
+        h = _P()
+        st = L.rmq_server_create(ctypes.byref(cfg), ctypes.byref(h))
+        if st != RMQ_OK:
+            raise RMQError(st, "rmq_server_create")
+        self._h = h
+        self._keep = {}
+
+    def register_generated(self, n: int, seed: int) -> int:
+        out = _U64()
+        st = _bind_server().rmq_server_register_generated(self._h, n, seed, ctypes.byref(out))
+        if st != RMQ_OK:
+            raise RMQError(st, "rmq_server_register_generated")
+        return int(out.value)
+
+    def register_host(self, values: np.ndarray) -> int:
+        values = np.ascontiguousarray(values, dtype=np.float32)
+        out = _U64()
+        st = _bind_server().rmq_server_register_host(self._h, values.ctypes.data, values.size, ctypes.byref(out))
+        if st != RMQ_OK:
+            raise RMQError(st, "rmq_server_register_host")
+        self._keep[("array", int(out.value))] = values
+        return int(out.value)
+
+    def submit(self, array_id: int, lr: np.ndarray, out_idx: np.ndarray | None = None,
+               out_min: np.ndarray | None = None) -> int:
+        assert lr.dtype == np.uint32 and lr.flags.c_contiguous
+        rid = _U64()
+        st = _bind_server().rmq_server_submit(
+            self._h, array_id, lr.ctypes.data, lr.size // 2,
+            out_idx.ctypes.data if out_idx is not None else None,
+            out_min.ctypes.data if out_min is not None else None, ctypes.byref(rid))
+        if st != RMQ_OK:
+            raise RMQError(st, "rmq_server_submit")
+        self._keep[("req", int(rid.value))] = (lr, out_idx, out_min)
+        return int(rid.value)
+
+    def wait(self, request_id: int, timeout_ms: int = -1) -> tuple[int, float]:
+        lat = ctypes.c_double()
+        st = _bind_server().rmq_server_wait(self._h, request_id, timeout_ms, ctypes.byref(lat))
+        if st != RMQ_ERR_TIMEOUT:
+            self._keep.pop(("req", request_id), None)
+        return st, float(lat.value)
+
+    def drain(self, timeout_ms: int = -1) -> None:
+        st = _bind_server().rmq_server_drain(self._h, timeout_ms)
+        if st != RMQ_OK:
+            raise RMQError(st, "rmq_server_drain")
+
+    def replay(self, events: np.ndarray, lr: np.ndarray, out_idx: np.ndarray, out_min: np.ndarray):
+        assert events.dtype == TRACE_DTYPE
+        lat = np.empty(events.size, dtype=np.float64)
+        wall = ctypes.c_double()
+        st = _bind_server().rmq_server_replay(self._h, events.ctypes.data, events.size, lr.ctypes.data,
+                                              out_idx.ctypes.data if out_idx is not None else None,
+                                              out_min.ctypes.data if out_min is not None else None,
+                                              lat.ctypes.data, ctypes.byref(wall))
+        if st != RMQ_OK:
+            raise RMQError(st, "rmq_server_replay")
+        return lat, float(wall.value)
+
+    def stats(self) -> dict:
+        s = ServerStats()
+        st = _bind_server().rmq_server_get_stats(self._h, ctypes.byref(s))
+        if st != RMQ_OK:
+            raise RMQError(st, "rmq_server_get_stats")
+        return s.as_dict()
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            _bind_server().rmq_server_destroy(self._h)
+            self._h = _P()
+            self._keep.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

@@ -15,6 +15,7 @@ from oracle import oracle
 HEADERS = {
     "rmq_gb300.h": R.LIB_PATH,
     "rmq_gb300_batch.h": R.LIB_PATH,
+    "rmq_gb300_serve.h": R.LIB_PATH,
     "rmq_gb300_gen.h": R.GEN_PATH,
 }
 

@@ -1,0 +1,113 @@
+"""The query server (GPU): results identical alone and in the mix and equal
+to the oracle; coalescing into shared batches; eviction and re-admission
+under a small HBM budget; invalid queries reported per request."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import rmq_gb300 as R
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def _queries(rng, n, q):
+    length = np.minimum(n, np.exp(rng.normal(np.log(max(2.0, n / 50)), 1.2, q)).astype(np.int64) + 1)
+    l = (rng.random(q) * (n - length + 1)).astype(np.int64)
+    return np.ascontiguousarray(np.stack([l, l + length - 1], 1).astype(np.uint32))
+
+
+def test_same_alone_and_in_mix(cuda):
+    rng = np.random.default_rng(5)
+    sizes = [1, 7, 100, 4099, 65_537, 1 << 20, 300_001, 8192, 77, 1 << 18]
+    arrays = []
+    for n in sizes:
+        a = (rng.integers(0, 40, n) / 3).astype(np.float32)  # ties
+        arrays.append(a)
+    reqs = []
+    for i in range(80):
+        aid = int(rng.integers(0, len(sizes)))
+        reqs.append((aid, _queries(rng, sizes[aid], int(rng.integers(1, 5000)))))
+    with R.Server(hbm_budget_bytes=1 << 30, slots=4) as srv:
+        ids = [srv.register_host(a) for a in arrays]
+        assert ids == list(range(len(sizes)))
+        alone = []
+        for aid, qs in reqs:
+            oi = np.empty(qs.shape[0], np.uint32)
+            om = np.empty(qs.shape[0], np.float32)
+            st, lat = srv.wait(srv.submit(aid, qs, oi, om))
+            assert st == R.RMQ_OK and lat > 0
+            alone.append((oi, om))
+        mix = []
+        rids = []
+        for aid, qs in reqs:
+            oi = np.empty(qs.shape[0], np.uint32)
+            om = np.empty(qs.shape[0], np.float32)
+            rids.append(srv.submit(aid, qs, oi, om))
+            mix.append((oi, om))
+        srv.drain()
+        for rid in rids:
+            assert srv.wait(rid)[0] == R.RMQ_OK
+        stats = srv.stats()
+    assert stats["max_requests_per_batch"] > 1  # the mix was coalesced
+    for (aid, qs), (ai, am), (mi, mm) in zip(reqs, alone, mix):
+        assert np.array_equal(ai, mi) and ai.tobytes() == mi.tobytes()
+        assert am.tobytes() == mm.tobytes()
+        assert np.array_equal(ai, oracle.rmq_argmin(arrays[aid], qs))
+        assert am.tobytes() == oracle.rmq_min(arrays[aid], qs).tobytes()
+
+
+def test_eviction_and_readmission(cuda):
+    import torch
+    rng = np.random.default_rng(6)
+    n = 1 << 20  # 4 MiB of values + levels per array
+    seeds = [11, 12, 13, 14, 15, 16]
+    with R.Server(hbm_budget_bytes=16 << 20, slots=2) as srv:  # room for ~3 arrays
+        ids = [srv.register_generated(n, s) for s in seeds]
+        expected = {}
+        for aid, seed in zip(ids, seeds):
+            v = torch.empty(n, dtype=torch.float32, device=cuda)
+            R.gen_values_device(v, seed)
+            torch.cuda.synchronize()
+            expected[aid] = v.cpu().numpy()
+        for rnd in range(3):
+            for aid in ids:
+                qs = _queries(rng, n, 2000)
+                oi = np.empty(qs.shape[0], np.uint32)
+                om = np.empty(qs.shape[0], np.float32)
+                st, _ = srv.wait(srv.submit(aid, qs, oi, om))
+                assert st == R.RMQ_OK
+                assert np.array_equal(oi, oracle.rmq_argmin(expected[aid], qs))
+                assert om.tobytes() == oracle.rmq_min(expected[aid], qs).tobytes()
+        stats = srv.stats()
+    assert stats["evictions"] > 0 and stats["readmissions"] > 0
+    assert stats["resident_bytes"] <= 16 << 20
+
+
+def test_invalid_query_and_replay(cuda):
+    rng = np.random.default_rng(7)
+    a = rng.random(1000).astype(np.float32)
+    with R.Server(hbm_budget_bytes=64 << 20) as srv:
+        aid = srv.register_host(a)
+        qs = np.array([[0, 999], [10, 5], [0, 1000]], dtype=np.uint32)
+        oi = np.empty(3, np.uint32)
+        om = np.empty(3, np.float32)
+        st, _ = srv.wait(srv.submit(aid, qs, oi, om))
+        assert st == R.RMQ_ERR_QUERY_RANGE
+        assert oi[0] == np.argmin(a) and oi[1] == R.NO_POS and oi[2] == R.NO_POS and np.isnan(om[1])
+        # a small replayed stream: a registration and requests before and after it
+        lr = _queries(rng, 1000, 3000)
+        ev = np.zeros(4, dtype=R.TRACE_DTYPE)
+        ev["t_arrival_s"] = [0.0, 0.001, 0.002, 0.003]
+        ev["kind"] = [0, 1, 0, 0]
+        ev["array_id"] = [aid, 0, aid, 1]
+        ev["n"] = [0, 1000, 0, 0]
+        ev["seed"] = [0, 3, 0, 0]
+        ev["q_offset"] = [0, 0, 1000, 2000]
+        ev["q"] = [1000, 0, 1000, 1000]
+        out_i = np.empty(3000, np.uint32)
+        out_m = np.empty(3000, np.float32)
+        lat, wall = srv.replay(ev, lr, out_i, out_m)
+        assert lat[1] == -1 and (lat[[0, 2, 3]] > 0).all() and wall > 0
+        assert np.array_equal(out_i[:2000], oracle.rmq_argmin(a, lr[:2000]))
