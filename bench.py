@@ -363,6 +363,34 @@ def run_ours(args, ws, rank, local):
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(a, qs, args.cpu_budget)
 
+    # The reference's own CL / VL kernels (compiled from its sources for
+    # sm_103a, oracle/_ref) on the same GPU and inputs: minima only, as the
+    # reference has no hierarchical argmin.
+    reference_gpu = None
+    if not args.no_reference_gpu:
+        from oracle import ref_gpu
+        if not ref_gpu.available():
+            reference_gpu = {"unavailable": "reference kernels not built (reference sources absent at build)"}
+        elif args.n % 4:
+            reference_gpu = {"unavailable": "n % 4 != 0 (the reference VL kernel reads whole float4s)"}
+        else:
+            reference_gpu = {}
+            ours_min = out_min.clone()
+            for variant, t in (("cl", 64), ("vl", 32), ("cl", args.t), ("vl", args.t)):
+                key = f"{variant}_t{t}"
+                if key in reference_gpu:
+                    continue
+                with torch.cuda.stream(stream):
+                    qps, ref_out = ref_gpu.time_reference(dv, dq, variant, t, steps=args.steps, warmup=3)
+                reference_gpu[key] = {"queries_per_s": qps,
+                                      "minima_equal_ours": bool(torch.equal(ref_out.view(torch.int32),
+                                                                            ours_min.view(torch.int32)))}
+                del ref_out
+            best = max(v["queries_per_s"] for v in reference_gpu.values())
+            reference_gpu["best_queries_per_s"] = best
+            reference_gpu["ours_min_only_vs_best"] = min_only_qps / best
+            reference_gpu["ours_min_argmin_vs_best"] = value / ws / best
+
     build_bytes = 4 * args.n + 8 * sum(info.sizes()[1:])
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -376,6 +404,7 @@ def run_ours(args, ws, rank, local):
         "gpu_launches": args.steps,
         "parity_sample_ok": parity,
         "min_only_queries_per_s": min_only_qps,
+        "reference_gpu": reference_gpu,
         "hierarchy": {"variant": ["auto", "cl", "vl"][info.variant], "rf": 1 << info.rf_log,
                       "t": int(info.scan_threshold), "levels": int(info.num_levels),
                       "lanes": int(info.lanes), "level_bytes": int(info.level_bytes),
@@ -743,6 +772,7 @@ def parse_args(argv=None):
     ap.add_argument("--e2e-chunk", dest="e2e_chunk", type=int, default=1 << 22)
     ap.add_argument("--cpu-budget", dest="cpu_budget", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", dest="no_cpu_baseline", action="store_true")
+    ap.add_argument("--no-reference-gpu", dest="no_reference_gpu", action="store_true")
     ap.add_argument("--ref-step-queries", dest="ref_step_queries", type=int, default=1 << 14)
     args = ap.parse_args(argv)
     args.warmup = max(3, args.warmup)  # timing rule: at least 3 untimed warm-up steps

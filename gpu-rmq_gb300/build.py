@@ -132,7 +132,7 @@ def build_reference(force: bool = False) -> Path | None:
     ref = Path(os.environ.get("RMQ_REFERENCE_ROOT", "/root/reference"))
     if not (ref / "src" / "cpu_methods.h").exists():
         return None
-    deps = [ORACLE / "ref_harness.cu", ORACLE / "build_ref.sh"]
+    deps = [ORACLE / "ref_harness.cu", ORACLE / "ref_gpu_harness.cu", ORACLE / "build_ref.sh"]
     if force or _stale(REF_LIB, deps):
         _run(["bash", str(ORACLE / "build_ref.sh"), str(ref)])
     return REF_LIB
