@@ -30,6 +30,7 @@ struct rmq_handle {
     int l2_persist = 0;
     int validate = 0;
     size_t persist_bytes = 0;
+    float persist_hit_ratio = 1.f;
     float build_ms = 0.f;
     std::mutex validate_mu;
 };
@@ -181,8 +182,11 @@ int rmq_build(const float* d_values, uint64_t n, const rmq_config* cfg, rmq_stre
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     cudaError_t e = cudaSuccess;
     if (h->lay.num_levels > 1) {
-        e = cudaMalloc(&h->val_buf, h->lay.total * sizeof(float));
-        if (e == cudaSuccess && h->with_index) e = cudaMalloc(&h->idx_buf, h->lay.total * sizeof(uint32_t));
+        // One allocation: level values, then argmin indices, so that a single
+        // L2 access-policy window can cover both.
+        const size_t entries = h->lay.total * (h->with_index ? 2 : 1);
+        e = cudaMalloc(&h->val_buf, entries * sizeof(float));
+        if (e == cudaSuccess && h->with_index) h->idx_buf = reinterpret_cast<uint32_t*>(h->val_buf + h->lay.total);
     }
     if (e == cudaSuccess) e = cudaMalloc(&h->err, sizeof(uint32_t));
     if (e != cudaSuccess) {
@@ -211,14 +215,17 @@ int rmq_build(const float* d_values, uint64_t n, const rmq_config* cfg, rmq_stre
         int max_persist = 0, max_window = 0;
         cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, h->device);
         cudaDeviceGetAttribute(&max_window, cudaDevAttrMaxAccessPolicyWindowSize, h->device);
-        size_t bytes = h->lay.total * sizeof(float);
+        size_t bytes = h->lay.total * (sizeof(float) + (h->idx_buf ? sizeof(uint32_t) : 0));
         if (bytes > size_t(max_window)) bytes = size_t(max_window);
-        if (bytes > size_t(max_persist)) bytes = size_t(max_persist);
-        if (bytes > 0) {
+        if (bytes > 0 && max_persist > 0) {
+            // Set-aside for persisting lines: the window, up to the device maximum
+            // (a context-wide limit, kept if a larger one is already set).
+            const size_t want = bytes < size_t(max_persist) ? bytes : size_t(max_persist);
             size_t cur = 0;
             cudaDeviceGetLimit(&cur, cudaLimitPersistingL2CacheSize);
-            if (cur < bytes) cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, bytes);
+            if (cur < want) cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, want);
             h->persist_bytes = bytes;
+            h->persist_hit_ratio = float(want) / float(bytes);
         }
         cudaGetLastError();
     }
@@ -255,6 +262,7 @@ static int query_common(const rmq_handle* hc, const uint32_t* d_lr, uint64_t q, 
     a.rf_log = h->lay.rf_log;
     a.persist_base = h->persist_bytes ? h->val_buf : nullptr;
     a.persist_bytes = h->persist_bytes;
+    a.persist_hit_ratio = h->persist_hit_ratio;
 
     if (!h->validate) {
         a.err = nullptr;
@@ -310,7 +318,6 @@ void rmq_destroy(rmq_handle* h) {
     {
         DeviceGuard guard(h->device);
         if (h->val_buf) cudaFree(h->val_buf);
-        if (h->idx_buf) cudaFree(h->idx_buf);
         if (h->err) cudaFree(h->err);
         cudaGetLastError();
     }

@@ -30,6 +30,7 @@ struct QueryArgs {
     uint32_t rf_log;
     const void* persist_base;   // L2 access-policy window (null = none)
     size_t persist_bytes;
+    float persist_hit_ratio;
 };
 
 cudaError_t launch_query(const QueryArgs& a, cudaStream_t s);

@@ -262,7 +262,7 @@ static cudaError_t launch_with_window(K kernel, uint32_t grid, const QueryArgs& 
         attr[0].id = cudaLaunchAttributeAccessPolicyWindow;
         attr[0].val.accessPolicyWindow.base_ptr = const_cast<void*>(a.persist_base);
         attr[0].val.accessPolicyWindow.num_bytes = a.persist_bytes;
-        attr[0].val.accessPolicyWindow.hitRatio = 1.0f;
+        attr[0].val.accessPolicyWindow.hitRatio = a.persist_hit_ratio;
         attr[0].val.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
         attr[0].val.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
         cfg.attrs = attr;
