@@ -47,3 +47,27 @@ def test_cpu_algorithms_and_csv(tmp_path, alg):
     row = lines[1].split(",")
     assert len(row) == len(lines[0].split(","))
     assert row[-5] == "-1"  # checkResult: no check ran
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("alg,extra", [
+    (22, ["--variant", "vl"]), (22, ["--variant", "cl"]), (122, ["--variant", "auto"]),
+    (122, ["--variant", "cl", "--rf_log", "5", "--lanes", "16"]), (2, []), (102, []),
+])
+@pytest.mark.parametrize("check", ["--check", "--randTrivialCheck", "--trivialCheck"])
+def test_gpu_algorithms_pass_checks(cuda, tmp_path, alg, extra, check):
+    csv = tmp_path / "t.csv"
+    r = run(1 << 20, 1 << 16, -6, alg, "--seed", 913, "--reps", 3, "--log_bs", 10, check,
+            f"--save-time={csv}", *extra)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    assert "pass" in r.stdout and "failed" not in r.stdout
+    row = csv.read_text().splitlines()[1].split(",")
+    code = int(row[-5])
+    assert code == {"--check": 1, "--trivialCheck": 3, "--randTrivialCheck": 5}[check]
+
+
+@pytest.mark.gpu
+def test_gpu_large_mixed_ties_check(cuda):
+    r = run(1 << 24, 1 << 20, -8, 122, "--seed", 7, "--reps", 2, "--log_bs", 6, "--ties", "0.01",
+            "--randTrivialCheck")
+    assert r.returncode == 0 and "pass" in r.stdout, r.stdout[-2000:]
