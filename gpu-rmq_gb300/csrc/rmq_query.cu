@@ -11,10 +11,9 @@
 // Two work distributions share that descent:
 //   VL  one thread per query, 256-bit sector loads (reference alg 20,
 //       kernel_hierarchical_vector_load, src/xxx.h:883-930, which uses float4);
-//   CL  a tile of G lanes per query (reference alg 16, xxx_query,
-//       src/xxx.h:124-200, where a tile answers its queries one after the
-//       other); here the lanes split the query's pieces by level so all
-//       loads of one query are in flight together.
+//   CL  a tile of G lanes answers its G queries one after another, the lanes
+//       sharing each query's sectors (reference alg 16, xxx_query,
+//       src/xxx.h:124-200).
 #include "rmq_internal.h"
 #include "rmq_vl.cuh"
 
@@ -30,167 +29,157 @@ query_vl_kernel(Levels lv, const uint2* __restrict__ qs, uint32_t q, float* __re
 }
 
 // ---------------------------------------------------------------------------
-// CL: a tile of G lanes per query, level-parallel
+// CL: a tile of G lanes per query, queries of the tile one after another
 //
-// Lane j of the tile owns the pieces of side (j & 1) (0 = left, 1 = right) at
-// levels j/2, j/2 + G/2, ... and the sectors j, j + G, ... of the final piece.
-// Every lane derives the descent (pure index arithmetic, no loads), then all
-// of its loads are issued together, so a query costs one memory round trip
-// for all levels instead of one per level.  The tile combines lane results by
-// (value, order key), where the key orders pieces by position: left pieces by
-// ascending level, then the final piece's sectors, then right pieces by
-// descending level; the lowest key among equal values is the first
-// occurrence.  The winning lane re-reads its sector, takes its first entry
-// equal to the minimum and, for a coarse level, loads the stored index.
+// As in the reference's xxx_query (src/xxx.h:124-200), a tile loads its G
+// queries (one per lane, coalesced) and answers them one after another; the
+// lanes share the work of each query.  Here the unit of sharing is a 32-byte
+// sector: at every level the sectors of the left piece, then of the right
+// piece, are dealt to the lanes (rf = 32 with G = 8: one 256-bit load per lane
+// per level), and the final piece's sectors likewise.  Each lane keeps the
+// running minimum of its sectors and, for argmin, its first sector holding it
+// under a position key (left pieces by ascending level, the final piece, right
+// pieces by descending level; sectors ascending inside a piece).  The tile
+// reduces the minimum, then the lowest key among lanes holding it; that lane
+// re-reads its sector, takes the first entry equal to the minimum and, for a
+// coarse level, loads the stored index.
 // ---------------------------------------------------------------------------
-constexpr uint32_t kKeyNone = 0xFFFFFFFFu;
-constexpr uint32_t kKeyFinal = 64u;  // keys of final sectors start here (levels < 20)
-
 struct LaneBest {
     float v;
-    uint32_t key;
+    uint64_t key;   // (group << 32) | sector index inside the piece
     uint32_t s;     // sector start
     uint32_t meta;  // level | jlo << 8 | jhi << 16
 };
 
+constexpr uint64_t kKeyNone = ~uint64_t(0);
+constexpr uint32_t kGroupFinal = 64u;  // left pieces use groups 0..19, right 128 + (19 - k)
+
 template <bool ARGMIN>
-__device__ __forceinline__ void lane_take(LaneBest& b, float sm, uint32_t key, uint32_t s, uint32_t meta) {
+__device__ __forceinline__ void cl_sector(const Levels& lv, uint32_t k, uint32_t s, uint32_t lo, uint32_t hi,
+                                          uint64_t key, const L2Policies& pol, LaneBest& b) {
+    const uint32_t jlo = s < lo ? lo - s : 0u;
+    const uint32_t jhi = hi - s < 8u ? hi - s : 8u;
+    float v[8];
+    load_level_sector(lv, k, s, pol, v);
+    const float sm = sector_min(v, jlo, jhi);
     if (ARGMIN) {
         if (sm < b.v || (sm == b.v && key < b.key)) {
             b.v = sm;
             b.key = key;
             b.s = s;
-            b.meta = meta;
+            b.meta = k | (jlo << 8) | (jhi << 16);
         }
     } else {
         b.v = fminf(b.v, sm);
     }
 }
 
-// One sector of level k restricted to [lo, hi).
-template <bool ARGMIN>
-__device__ __forceinline__ void cl_sector(const Levels& lv, uint32_t k, uint32_t s, uint32_t lo, uint32_t hi,
-                                          uint32_t key, const L2Policies& pol, LaneBest& b) {
-    const uint32_t jlo = s < lo ? lo - s : 0u;
-    const uint32_t jhi = hi - s < 8u ? hi - s : 8u;
-    float v[8];
-    load_level_sector(lv, k, s, pol, v);
-    lane_take<ARGMIN>(b, sector_min(v, jlo, jhi), key, s, k | (jlo << 8) | (jhi << 16));
+// The tile's lanes scan the sectors of [alo, ahi) (group ga) followed by the
+// sectors of [blo, bhi) (group gb) of level k; lane `lane` takes sectors
+// lane, lane + G, ... of that combined list.
+template <int G, bool ARGMIN>
+__device__ __forceinline__ void cl_pair(const Levels& lv, uint32_t k, uint32_t alo, uint32_t ahi, uint32_t ga,
+                                        uint32_t blo, uint32_t bhi, uint32_t gb, uint32_t lane,
+                                        const L2Policies& pol, LaneBest& b) {
+    const uint32_t a0 = alo & ~7u, b0 = blo & ~7u;
+    const uint32_t na = ahi > alo ? ((ahi - a0 + 7u) >> 3) : 0u;
+    const uint32_t nb = bhi > blo ? ((bhi - b0 + 7u) >> 3) : 0u;
+    for (uint32_t j = lane; j < na + nb; j += G) {
+        const bool in_a = j < na;
+        const uint32_t idx = in_a ? j : j - na;
+        const uint32_t s = (in_a ? a0 : b0) + 8u * idx;
+        const uint64_t key = (uint64_t(in_a ? ga : gb) << 32) | idx;
+        cl_sector<ARGMIN>(lv, k, s, in_a ? alo : blo, in_a ? ahi : bhi, key, pol, b);
+    }
 }
 
 template <int R, int G, bool ARGMIN>
-__device__ __forceinline__ void cl_lane_work(const Levels& lv, uint32_t l, uint32_t r, uint32_t lane,
-                                             const L2Policies& pol, LaneBest& b) {
+__device__ __forceinline__ void cl_query(const Levels& lv, uint32_t l, uint32_t r, uint32_t lane,
+                                         const L2Policies& pol, LaneBest& b) {
     constexpr uint32_t RF = 1u << R;
-    constexpr uint32_t PAIRS = G / 2u;
-    const uint32_t my_level = lane >> 1;
-    const bool right = (lane & 1u) != 0u;
-    // Descent: stop level s and final piece [l, r) at level s; this lane's
-    // boundary pieces are recorded as they are passed (at most
-    // ceil(19 / PAIRS) of them; pieces are processed after the loop).
-    constexpr uint32_t kMaxPieces = (19u + PAIRS - 1u) / PAIRS;
-    uint32_t plo[kMaxPieces], phi[kMaxPieces];
-    uint32_t np = 0;
     uint32_t k = 0;
     while (k + 1 < lv.num_levels && r - l > 2u * RF) {
         const uint32_t nl = (l + RF - 1) & ~(RF - 1);
         const uint32_t pr = r & ~(RF - 1);
-        if (k % PAIRS == my_level) {
-#pragma unroll
-            for (uint32_t i = 0; i < kMaxPieces; ++i) {  // constant indices keep plo/phi in registers
-                if (np == i) {
-                    plo[i] = right ? pr : l;
-                    phi[i] = right ? r : nl;
-                }
-            }
-            ++np;
-        }
+        cl_pair<G, ARGMIN>(lv, k, l, nl, k, pr, r, 128u + (19u - k), lane, pol, b);
         l = nl >> R;
         r = pr >> R;
         ++k;
     }
-    // Final piece sectors: all independent of the pieces, issued alongside.
-    const uint32_t f0 = l & ~7u;
-    for (uint32_t s = f0 + 8u * lane; s < r; s += 8u * G) {
-        cl_sector<ARGMIN>(lv, k, s, l, r, kKeyFinal + ((s - f0) >> 3), pol, b);
-    }
-#pragma unroll
-    for (uint32_t i = 0; i < kMaxPieces; ++i) {
-        if (i < np && phi[i] > plo[i]) {
-            const uint32_t lvl = my_level + i * PAIRS;
-            const uint32_t key = right ? (kKeyNone - 1u - lvl) : lvl;
-            for (uint32_t s = plo[i] & ~7u; s < phi[i]; s += 8u)
-                cl_sector<ARGMIN>(lv, lvl, s, plo[i], phi[i], key, pol, b);
-        }
-    }
+    cl_pair<G, ARGMIN>(lv, k, l, r, kGroupFinal, 0u, 0u, 0u, lane, pol, b);
 }
 
 template <int R, int G, bool ARGMIN>
 __global__ void __launch_bounds__(256)
 query_cl_kernel(Levels lv, const uint2* __restrict__ qs, uint32_t q, float* __restrict__ out_min,
                 uint32_t* __restrict__ out_idx, uint32_t* __restrict__ err) {
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t lane = threadIdx.x & (G - 1u);
-    const uint32_t qi = (blockIdx.x * blockDim.x + threadIdx.x) / G;
     const uint32_t wl = threadIdx.x & 31u;
     const uint32_t mask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (wl - lane));
-    if (qi >= q) return;  // uniform across the tile
-    const uint2 Q = ld_query(qs + qi);
-    if (Q.x > Q.y || Q.y >= lv.size[0]) {
-        if (lane == 0) {
-            if (out_min != nullptr) st_stream(out_min + qi, f_nan());
-            if (ARGMIN) st_stream(out_idx + qi, kNoPos);
-            if (err != nullptr) atomicAdd(err, 1u);
-        }
-        return;
-    }
+    const uint32_t base = tid - lane;  // first query of the tile
     const L2Policies pol = make_policies();
-    const uint32_t l = Q.x, r = Q.y + 1;
-    LaneBest b{f_inf(), kKeyNone, 0u, 0u};
-    bool need_locate = ARGMIN;
-    cl_lane_work<R, G, ARGMIN>(lv, l, r, lane, pol, b);
-    float m = b.v;
-#pragma unroll
-    for (int o = 1; o < G; o <<= 1) m = fminf(m, __shfl_xor_sync(mask, m, o, G));
-    if (!ARGMIN) {
-        if (m != 0.0f) {
-            if (lane == 0) st_stream(out_min + qi, m);
-            return;
-        }
-        // A zero minimum may be -0.0 or +0.0: locate the first one for its bits.
-        b = LaneBest{f_inf(), kKeyNone, 0u, 0u};
-        cl_lane_work<R, G, true>(lv, l, r, lane, pol, b);
-        need_locate = true;
+
+    uint2 Q = make_uint2(1u, 0u);
+    if (tid < q) Q = ld_query(qs + tid);
+    const bool valid = tid < q && Q.x <= Q.y && Q.y < lv.size[0];
+    if (tid < q && !valid) {
+        if (out_min != nullptr) st_stream(out_min + tid, f_nan());
+        if (ARGMIN) st_stream(out_idx + tid, kNoPos);
+        if (err != nullptr) atomicAdd(err, 1u);
     }
-    if (need_locate) {
-        // The winner: lowest key among the lanes holding the minimum.
-        uint32_t key = (b.v == m) ? b.key : kKeyNone;
+    const uint32_t vmask = __ballot_sync(mask, valid) >> (wl - lane);  // the tile's valid queries
+    for (uint32_t j = 0; j < G; ++j) {
+        if (((vmask >> j) & 1u) == 0u) continue;  // uniform across the tile
+        const uint32_t l = __shfl_sync(mask, Q.x, j, G);
+        const uint32_t r = __shfl_sync(mask, Q.y, j, G) + 1u;
+        LaneBest b{f_inf(), kKeyNone, 0u, 0u};
+        cl_query<R, G, ARGMIN>(lv, l, r, lane, pol, b);
+        float m = b.v;
 #pragma unroll
-        for (int o = 1; o < G; o <<= 1) key = min(key, __shfl_xor_sync(mask, key, o, G));
-        if (key == kKeyNone) {
-            // No entry compared equal to the minimum: NaN inputs only (outside
-            // the contract); the scan's answer is the first entry.
-            if (lane == 0) {
-                if (out_idx != nullptr) st_stream(out_idx + qi, l);
-                if (out_min != nullptr) st_stream(out_min + qi, __ldg(lv.val[0] + l));
+        for (int o = 1; o < G; o <<= 1) m = fminf(m, __shfl_xor_sync(mask, m, o, G));
+        bool locate = ARGMIN;
+        if (!ARGMIN) {
+            if (m != 0.0f) {
+                if (lane == j) st_stream(out_min + base + j, m);
+                continue;
             }
-            return;
+            // A zero minimum may be -0.0 or +0.0: locate the first one for its bits.
+            b = LaneBest{f_inf(), kKeyNone, 0u, 0u};
+            cl_query<R, G, true>(lv, l, r, lane, pol, b);
+            locate = true;
         }
-        if (b.key == key && b.v == m) {
-            const uint32_t k = b.meta & 0xffu;
-            const uint32_t jlo = (b.meta >> 8) & 0xffu;
-            const uint32_t jhi = (b.meta >> 16) & 0xffu;
-            float v[8];
-            load_level_sector(lv, k, b.s, pol, v);
-            uint32_t j = jlo;
+        if (locate) {
+            uint64_t key = (b.v == m) ? b.key : kKeyNone;
 #pragma unroll
-            for (int jj = 7; jj >= 0; --jj)
-                if (uint32_t(jj) >= jlo && uint32_t(jj) < jhi && v[jj] == m) j = uint32_t(jj);
-            float val = v[0];
+            for (int o = 1; o < G; o <<= 1) {
+                const uint64_t other = __shfl_xor_sync(mask, key, o, G);
+                key = other < key ? other : key;
+            }
+            if (key == kKeyNone) {
+                // No entry compared equal to the minimum: NaN inputs only
+                // (outside the contract); the scan's answer is the first entry.
+                if (lane == j) {
+                    if (out_idx != nullptr) st_stream(out_idx + base + j, l);
+                    if (out_min != nullptr) st_stream(out_min + base + j, __ldg(lv.val[0] + l));
+                }
+            } else if (b.key == key && b.v == m) {
+                const uint32_t k = b.meta & 0xffu;
+                const uint32_t jlo = (b.meta >> 8) & 0xffu;
+                const uint32_t jhi = (b.meta >> 16) & 0xffu;
+                float v[8];
+                load_level_sector(lv, k, b.s, pol, v);
+                uint32_t jj = jlo;
 #pragma unroll
-            for (int jj = 1; jj < 8; ++jj) val = (uint32_t(jj) == j) ? v[jj] : val;
-            const uint32_t e = b.s + j;
-            if (out_idx != nullptr) st_stream(out_idx + qi, k == 0 ? e : ld_index(lv.idx[k] + e));
-            if (out_min != nullptr) st_stream(out_min + qi, val);
+                for (int t = 7; t >= 0; --t)
+                    if (uint32_t(t) >= jlo && uint32_t(t) < jhi && v[t] == m) jj = uint32_t(t);
+                float val = v[0];
+#pragma unroll
+                for (int t = 1; t < 8; ++t) val = (uint32_t(t) == jj) ? v[t] : val;
+                const uint32_t e = b.s + jj;
+                if (out_idx != nullptr) st_stream(out_idx + base + j, k == 0 ? e : ld_index(lv.idx[k] + e));
+                if (out_min != nullptr) st_stream(out_min + base + j, val);
+            }
         }
     }
 }
@@ -282,7 +271,7 @@ static cudaError_t launch_query_r(const QueryArgs& a, cudaStream_t s) {
         return argmin ? launch_with_window(query_vl_kernel<R, true>, grid, a, s)
                       : launch_with_window(query_vl_kernel<R, false>, grid, a, s);
     }
-    const uint32_t grid = uint32_t((uint64_t(a.q) * uint64_t(a.lanes) + 255u) / 256u);
+    const uint32_t grid = (a.q + 255u) / 256u;
     switch (a.lanes) {
         case 4:
             return argmin ? launch_with_window(query_cl_kernel<R, 4, true>, grid, a, s)
