@@ -22,6 +22,8 @@ struct rmq_handle {
     const float* d_values = nullptr;
     float* val_buf = nullptr;
     uint32_t* idx_buf = nullptr;
+    uint64_t* idx_buf64 = nullptr;  // 64-bit handles
+    bool wide = false;
     uint32_t* err = nullptr;  // invalid-query counter (validate mode)
     int device = 0;
     int variant = RMQ_VARIANT_VL;
@@ -52,9 +54,11 @@ constexpr uint64_t kVlT = 32;
 // level-parallel CL kernel replicates the descent's index arithmetic on every
 // lane of the tile, which costs more than the memory round trips it saves).
 
-// Largest supported n: queries are uint32 pairs and the descent rounds r up by
-// at most rf - 1 without overflowing 32 bits.
+// Largest n of 32-bit handles: queries are uint32 pairs and the descent rounds
+// r up by at most rf - 1 without overflowing 32 bits.  64-bit handles take up
+// to 2^40 entries (4 TiB of values, far above any GPU's memory).
 constexpr uint64_t kMaxN = 0xFFFFFF00ull;
+constexpr uint64_t kMaxNWide = uint64_t(1) << 40;
 
 struct DeviceGuard {
     int prev = -1;
@@ -100,6 +104,7 @@ int resolve_config(uint64_t n, const rmq_config* cfg_in, int* variant, int* rf_l
 
 void fill_info(const Layout& lay, int variant, int lanes, rmq_info* info) {
     std::memset(info, 0, sizeof(*info));
+    info->index_bits = 32;
     info->num_levels = lay.num_levels;
     info->rf_log = lay.rf_log;
     info->variant = variant;
@@ -140,7 +145,7 @@ const char* rmq_strerror(int status) {
 int rmq_plan_layout(uint64_t n, uint64_t scan_threshold, int32_t rf_log, int32_t variant,
                     rmq_info* info) {
     if (info == nullptr || n == 0) return RMQ_ERR_ARG;
-    if (n > kMaxN) return RMQ_ERR_UNSUPPORTED;
+    if (n > kMaxNWide) return RMQ_ERR_UNSUPPORTED;
     rmq_config cfg;
     rmq_config_init(&cfg);
     cfg.variant = variant;
@@ -152,6 +157,7 @@ int rmq_plan_layout(uint64_t n, uint64_t scan_threshold, int32_t rf_log, int32_t
     if (st != RMQ_OK) return st;
     const Layout lay = rmq::plan_layout(n, t, uint32_t(r));
     fill_info(lay, v, g, info);
+    if (n > kMaxN) info->index_bits = 64;
     return RMQ_OK;
 }
 
@@ -161,11 +167,16 @@ int rmq_build(const float* d_values, uint64_t n, const rmq_config* cfg, rmq_stre
     *out = nullptr;
     if (d_values == nullptr || n == 0) return RMQ_ERR_ARG;
     if ((reinterpret_cast<uintptr_t>(d_values) & 31u) != 0) return RMQ_ERR_ARG;
-    if (n > kMaxN) return RMQ_ERR_UNSUPPORTED;
+    if (n > kMaxNWide) return RMQ_ERR_UNSUPPORTED;
     int v, r, g;
     uint64_t t;
     int st = resolve_config(n, cfg, &v, &r, &t, &g);
     if (st != RMQ_OK) return st;
+    const int bits = cfg != nullptr ? cfg->index_bits : 0;
+    if (bits != 0 && bits != 32 && bits != 64) return RMQ_ERR_ARG;
+    const bool wide = bits == 64 || n > kMaxN;
+    if (bits == 32 && n > kMaxN) return RMQ_ERR_UNSUPPORTED;
+    if (wide && v != RMQ_VARIANT_VL) return RMQ_ERR_UNSUPPORTED;  // 64-bit positions: VL only
 
     rmq_handle* h = new (std::nothrow) rmq_handle();
     if (h == nullptr) return RMQ_ERR_OOM;
@@ -174,6 +185,7 @@ int rmq_build(const float* d_values, uint64_t n, const rmq_config* cfg, rmq_stre
         return RMQ_ERR_CUDA;
     }
     h->lay = rmq::plan_layout(n, t, uint32_t(r));
+    h->wide = wide;
     h->d_values = d_values;
     h->variant = v;
     h->lanes = g;
@@ -186,9 +198,10 @@ int rmq_build(const float* d_values, uint64_t n, const rmq_config* cfg, rmq_stre
     if (h->lay.num_levels > 1) {
         // One allocation: level values, then argmin indices, so that a single
         // L2 access-policy window can cover both.
-        const size_t entries = h->lay.total * (h->with_index ? 2 : 1);
-        e = cudaMalloc(&h->val_buf, entries * sizeof(float));
-        if (e == cudaSuccess && h->with_index) h->idx_buf = reinterpret_cast<uint32_t*>(h->val_buf + h->lay.total);
+        const size_t idx_bytes = h->with_index ? (wide ? sizeof(uint64_t) : sizeof(uint32_t)) : 0;
+        e = cudaMalloc(&h->val_buf, h->lay.total * (sizeof(float) + idx_bytes));
+        if (e == cudaSuccess && h->with_index && !wide) h->idx_buf = reinterpret_cast<uint32_t*>(h->val_buf + h->lay.total);
+        if (e == cudaSuccess && h->with_index && wide) h->idx_buf64 = reinterpret_cast<uint64_t*>(h->val_buf + h->lay.total);
     }
     if (e == cudaSuccess) e = cudaMalloc(&h->err, sizeof(uint32_t));
     if (e != cudaSuccess) {
@@ -201,7 +214,9 @@ int rmq_build(const float* d_values, uint64_t n, const rmq_config* cfg, rmq_stre
     e = cudaEventCreate(&e0);
     if (e == cudaSuccess) e = cudaEventCreate(&e1);
     if (e == cudaSuccess) e = cudaEventRecord(e0, s);
-    if (e == cudaSuccess) e = rmq::launch_build(h->lay, d_values, h->val_buf, h->idx_buf, s);
+    if (e == cudaSuccess)
+        e = wide ? rmq::launch_build64(h->lay, d_values, h->val_buf, h->idx_buf64, s)
+                 : rmq::launch_build(h->lay, d_values, h->val_buf, h->idx_buf, s);
     if (e == cudaSuccess) e = cudaEventRecord(e1, s);
     if (e == cudaSuccess) e = cudaEventSynchronize(e1);
     if (e == cudaSuccess) e = cudaEventElapsedTime(&h->build_ms, e0, e1);
@@ -217,7 +232,8 @@ int rmq_build(const float* d_values, uint64_t n, const rmq_config* cfg, rmq_stre
         int max_persist = 0, max_window = 0;
         cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, h->device);
         cudaDeviceGetAttribute(&max_window, cudaDevAttrMaxAccessPolicyWindowSize, h->device);
-        size_t bytes = h->lay.total * (sizeof(float) + (h->idx_buf ? sizeof(uint32_t) : 0));
+        size_t bytes = h->lay.total * (sizeof(float) + (h->idx_buf ? sizeof(uint32_t) : 0) +
+                                       (h->idx_buf64 ? sizeof(uint64_t) : 0));
         if (bytes > size_t(max_window)) bytes = size_t(max_window);
         if (bytes > 0 && max_persist > 0) {
             // Set-aside for persisting lines: the window, up to the device maximum
@@ -235,12 +251,14 @@ int rmq_build(const float* d_values, uint64_t n, const rmq_config* cfg, rmq_stre
     return RMQ_OK;
 }
 
-static int query_common(const rmq_handle* hc, const uint32_t* d_lr, uint64_t q, float* d_min,
-                        uint32_t* d_argmin, rmq_stream_t stream) {
+static int query_common(const rmq_handle* hc, const void* d_lr, uint64_t q, float* d_min, void* d_argmin,
+                        bool wide_call, rmq_stream_t stream) {
     if (hc == nullptr) return RMQ_ERR_ARG;
+    if (hc->wide != wide_call) return RMQ_ERR_UNSUPPORTED;
     if (q == 0) return RMQ_OK;
-    if (q > 0xFFFFFFFFull) return RMQ_ERR_UNSUPPORTED;
-    if (d_lr == nullptr || (reinterpret_cast<uintptr_t>(d_lr) & 7u) != 0) return RMQ_ERR_ARG;
+    if (!wide_call && q > 0xFFFFFFFFull) return RMQ_ERR_UNSUPPORTED;
+    const uintptr_t qalign = wide_call ? 15u : 7u;
+    if (d_lr == nullptr || (reinterpret_cast<uintptr_t>(d_lr) & qalign) != 0) return RMQ_ERR_ARG;
     if (d_min == nullptr && d_argmin == nullptr) return RMQ_ERR_ARG;
     if (d_argmin != nullptr && !hc->with_index && hc->lay.num_levels > 1) return RMQ_ERR_NO_INDEX;
     rmq_handle* h = const_cast<rmq_handle*>(hc);
@@ -250,15 +268,29 @@ static int query_common(const rmq_handle* hc, const uint32_t* d_lr, uint64_t q, 
     rmq::QueryArgs a;
     std::memset(&a, 0, sizeof(a));
     for (uint32_t k = 0; k < h->lay.num_levels; ++k) {
-        a.lv.val[k] = k == 0 ? h->d_values : h->val_buf + h->lay.offset[k];
-        a.lv.idx[k] = (k == 0 || h->idx_buf == nullptr) ? nullptr : h->idx_buf + h->lay.offset[k];
-        a.lv.size[k] = uint32_t(h->lay.size[k]);
+        const float* val = k == 0 ? h->d_values : h->val_buf + h->lay.offset[k];
+        if (h->wide) {
+            a.lv64.val[k] = val;
+            a.lv64.idx[k] = (k == 0 || h->idx_buf64 == nullptr) ? nullptr : h->idx_buf64 + h->lay.offset[k];
+            a.lv64.size[k] = h->lay.size[k];
+        } else {
+            a.lv.val[k] = val;
+            a.lv.idx[k] = (k == 0 || h->idx_buf == nullptr) ? nullptr : h->idx_buf + h->lay.offset[k];
+            a.lv.size[k] = uint32_t(h->lay.size[k]);
+        }
     }
     a.lv.num_levels = h->lay.num_levels;
-    a.qs = reinterpret_cast<const uint2*>(d_lr);
-    a.q = uint32_t(q);
+    a.lv64.num_levels = h->lay.num_levels;
+    a.wide = h->wide;
+    a.q = q;
     a.out_min = d_min;
-    a.out_idx = d_argmin;
+    if (h->wide) {
+        a.qs64 = static_cast<const uint64_t*>(d_lr);
+        a.out_idx64 = static_cast<uint64_t*>(d_argmin);
+    } else {
+        a.qs = static_cast<const uint2*>(d_lr);
+        a.out_idx = static_cast<uint32_t*>(d_argmin);
+    }
     a.variant = h->variant;
     a.lanes = h->lanes;
     a.rf_log = h->lay.rf_log;
@@ -284,13 +316,25 @@ static int query_common(const rmq_handle* hc, const uint32_t* d_lr, uint64_t q, 
 int rmq_query(const rmq_handle* h, const uint32_t* d_lr, uint64_t q, float* d_min,
               rmq_stream_t stream) {
     if (d_min == nullptr) return RMQ_ERR_ARG;
-    return query_common(h, d_lr, q, d_min, nullptr, stream);
+    return query_common(h, d_lr, q, d_min, nullptr, false, stream);
 }
 
 int rmq_query_idx(const rmq_handle* h, const uint32_t* d_lr, uint64_t q, uint32_t* d_argmin,
                   float* d_min_or_null, rmq_stream_t stream) {
     if (d_argmin == nullptr) return RMQ_ERR_ARG;
-    return query_common(h, d_lr, q, d_min_or_null, d_argmin, stream);
+    return query_common(h, d_lr, q, d_min_or_null, d_argmin, false, stream);
+}
+
+int rmq_query64(const rmq_handle* h, const uint64_t* d_lr, uint64_t q, float* d_min,
+                rmq_stream_t stream) {
+    if (d_min == nullptr) return RMQ_ERR_ARG;
+    return query_common(h, d_lr, q, d_min, nullptr, true, stream);
+}
+
+int rmq_query_idx64(const rmq_handle* h, const uint64_t* d_lr, uint64_t q, uint64_t* d_argmin,
+                    float* d_min_or_null, rmq_stream_t stream) {
+    if (d_argmin == nullptr) return RMQ_ERR_ARG;
+    return query_common(h, d_lr, q, d_min_or_null, d_argmin, true, stream);
 }
 
 int rmq_scan_bruteforce(const float* d_values, uint64_t n, const uint32_t* d_lr, uint64_t q,
@@ -308,8 +352,10 @@ int rmq_scan_bruteforce(const float* d_values, uint64_t n, const uint32_t* d_lr,
 int rmq_get_info(const rmq_handle* h, rmq_info* info) {
     if (h == nullptr || info == nullptr) return RMQ_ERR_ARG;
     fill_info(h->lay, h->variant, h->lanes, info);
+    info->index_bits = h->wide ? 64 : 32;
     info->level_bytes = h->lay.num_levels > 1
-                            ? h->lay.total * (sizeof(float) + (h->idx_buf ? sizeof(uint32_t) : 0))
+                            ? h->lay.total * (sizeof(float) + (h->idx_buf ? sizeof(uint32_t) : 0) +
+                                              (h->idx_buf64 ? sizeof(uint64_t) : 0))
                             : 0;
     info->build_ms = h->build_ms;
     return RMQ_OK;

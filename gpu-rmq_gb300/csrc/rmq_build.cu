@@ -13,32 +13,23 @@
 
 namespace rmq {
 
-__device__ __forceinline__ void ld_sector_u32(const uint32_t* p, uint32_t (&v)[8]) {
-    asm(
-        "ld.global.nc.L1::no_allocate.v8.u32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]),
-          "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7])
-        : "l"(p));
-}
-
-// One output block per group of LPB = rf/8 lanes.
+// One output block per group of LPB = rf/8 lanes (P: position type).
 //   src, src_size : level k (level 0 = caller's array, not padded)
 //   src_idx       : level-0 indices of level k's entries (null for k = 0)
 //   src_padded    : src has at least round_up(src_size, 8) readable entries
-template <int R>
+template <int R, typename P>
 __global__ void __launch_bounds__(256)
-build_step_kernel(const float* __restrict__ src, const uint32_t* __restrict__ src_idx,
-                  uint32_t src_size, int src_padded, float* __restrict__ dst,
-                  uint32_t* __restrict__ dst_idx, uint32_t dst_size) {
+build_step_kernel(const float* __restrict__ src, const P* __restrict__ src_idx, P src_size, int src_padded,
+                  float* __restrict__ dst, P* __restrict__ dst_idx, P dst_size) {
     constexpr uint32_t LPB = (1u << R) / 8u;
-    const uint32_t gt = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t blk = gt / LPB;
-    const uint32_t sub = gt % LPB;
+    constexpr P kNone = IdxTraits<P>::none;
+    const uint64_t gt = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    const P blk = P(gt / LPB);
+    const uint32_t sub = uint32_t(gt % LPB);
 
-    Cand c;
-    cand_init(c);
+    VPT<P> c{f_inf(), kNone};
     if (blk < dst_size) {
-        const uint32_t s = (blk << R) + 8u * sub;
+        const P s = (blk << R) + 8u * sub;
         if (s < src_size) {
             float v[8];
             if (src_padded || s + 8u <= src_size) {
@@ -47,29 +38,26 @@ build_step_kernel(const float* __restrict__ src, const uint32_t* __restrict__ sr
 #pragma unroll
                 for (int j = 0; j < 8; ++j) v[j] = (s + j < src_size) ? src[s + j] : f_inf();
             }
-            uint32_t ix[8];
-            if (src_idx != nullptr) {
-                ld_sector_u32(src_idx + s, ix);  // level >= 1 buffers are padded
-            } else {
-#pragma unroll
-                for (int j = 0; j < 8; ++j) ix[j] = s + j;
-            }
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
-                if (s + j < src_size) cand_update(c, v[j], ix[j], 0);
+                if (s + j < src_size) vp_take(c, v[j], src_idx != nullptr ? __ldg(src_idx + s + j) : P(s + j));
             }
         }
     }
-    // Combine the LPB lanes of a block (groups never straddle a warp).
+    // Combine the LPB lanes of a block (groups never straddle a warp; the
+    // lanes' positions are disjoint, so equal values keep the lower one).
 #pragma unroll
     for (uint32_t o = 1; o < LPB; o <<= 1) {
         const float ov = __shfl_xor_sync(0xffffffffu, c.v, o);
-        const uint32_t op = __shfl_xor_sync(0xffffffffu, c.pos, o);
-        cand_update(c, ov, op, 0);
+        const P op = __shfl_xor_sync(0xffffffffu, c.p, o);
+        if (op != kNone && (c.p == kNone || ov < c.v || (ov == c.v && op < c.p))) {
+            c.v = ov;
+            c.p = op;
+        }
     }
     if (blk < dst_size && sub == 0) {
         dst[blk] = c.v;
-        if (dst_idx != nullptr) dst_idx[blk] = c.pos;
+        if (dst_idx != nullptr) dst_idx[blk] = c.p;
     }
 }
 
@@ -105,16 +93,16 @@ Layout plan_layout(uint64_t n, uint64_t t, uint32_t rf_log) {
 // The levels above are small; a single-CTA tail kernel finishes them (or
 // grid-wide build_step launches while they are still large).
 // ---------------------------------------------------------------------------
-template <int R>
+template <int R, typename P>
 __global__ void __launch_bounds__(kFusedThreads)
-build_fused_kernel(const float* __restrict__ a, uint32_t n, LevelOut out, uint32_t depth) {
+build_fused_kernel(const float* __restrict__ a, P n, LevelOutT<P> out, uint32_t depth) {
     __shared__ float sv[kTileSectors];
-    __shared__ uint32_t sp[kTileSectors];
+    __shared__ P sp[kTileSectors];
     fused_tile<R>(a, n, out, depth, blockIdx.x, sv, sp);
 }
 
-template <int R>
-__global__ void __launch_bounds__(1024) build_tail_kernel(LevelOut out, uint32_t from, uint32_t last) {
+template <int R, typename P>
+__global__ void __launch_bounds__(1024) build_tail_kernel(LevelOutT<P> out, uint32_t from, uint32_t last) {
     tail_levels<R>(out, from, last);
 }
 
@@ -143,19 +131,19 @@ int build_launch_count(const Layout& lay) {
     }
 }
 
-template <int R>
-static cudaError_t build_levels(const Layout& lay, const float* d_values, float* val_buf,
-                                uint32_t* idx_buf, cudaStream_t s) {
+template <int R, typename P>
+static cudaError_t build_levels(const Layout& lay, const float* d_values, float* val_buf, P* idx_buf,
+                                cudaStream_t s) {
     constexpr uint32_t LPB = (1u << R) / 8u;
     if (lay.num_levels < 2) return cudaSuccess;
-    LevelOut out;
+    LevelOutT<P> out;
     for (uint32_t k = 0; k < uint32_t(kMaxLevels); ++k) {
         out.val[k] = nullptr;
         out.idx[k] = nullptr;
         out.size[k] = 0;
     }
     for (uint32_t k = 0; k < lay.num_levels; ++k) {
-        out.size[k] = uint32_t(lay.size[k]);
+        out.size[k] = P(lay.size[k]);
         if (k > 0) {
             out.val[k] = val_buf + lay.offset[k];
             out.idx[k] = idx_buf == nullptr ? nullptr : idx_buf + lay.offset[k];
@@ -164,36 +152,47 @@ static cudaError_t build_levels(const Layout& lay, const float* d_values, float*
     uint32_t fused, steps;
     bool tail;
     plan_launches<R>(lay, &fused, &steps, &tail);
-    const uint32_t n = uint32_t(lay.size[0]);
+    const P n = P(lay.size[0]);
     const uint32_t tiles = uint32_t((uint64_t(n) + kTile - 1) / kTile);
-    build_fused_kernel<R><<<tiles, kFusedThreads, 0, s>>>(d_values, n, out, fused);
+    build_fused_kernel<R, P><<<tiles, kFusedThreads, 0, s>>>(d_values, n, out, fused);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     uint32_t k = fused;
     for (uint32_t i = 0; i < steps; ++i, ++k) {
-        const uint32_t dst_size = out.size[k + 1];
+        const P dst_size = out.size[k + 1];
         const uint64_t threads = uint64_t(dst_size) * LPB;
         const uint32_t grid = uint32_t((threads + 255) / 256);
-        build_step_kernel<R><<<grid, 256, 0, s>>>(out.val[k], out.idx[k], out.size[k], 1, out.val[k + 1],
-                                                 out.idx[k + 1], dst_size);
+        build_step_kernel<R, P><<<grid, 256, 0, s>>>(out.val[k], out.idx[k], out.size[k], 1, out.val[k + 1],
+                                                    out.idx[k + 1], dst_size);
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
     if (tail) {
-        build_tail_kernel<R><<<1, 1024, 0, s>>>(out, k, lay.num_levels - 1);
+        build_tail_kernel<R, P><<<1, 1024, 0, s>>>(out, k, lay.num_levels - 1);
         e = cudaGetLastError();
     }
     return e;
 }
 
-cudaError_t launch_build(const Layout& lay, const float* d_values, float* val_buf,
-                         uint32_t* idx_buf, cudaStream_t s) {
+template <typename P>
+static cudaError_t launch_build_p(const Layout& lay, const float* d_values, float* val_buf, P* idx_buf,
+                                  cudaStream_t s) {
     switch (lay.rf_log) {
-        case 3: return build_levels<3>(lay, d_values, val_buf, idx_buf, s);
-        case 4: return build_levels<4>(lay, d_values, val_buf, idx_buf, s);
-        case 5: return build_levels<5>(lay, d_values, val_buf, idx_buf, s);
+        case 3: return build_levels<3, P>(lay, d_values, val_buf, idx_buf, s);
+        case 4: return build_levels<4, P>(lay, d_values, val_buf, idx_buf, s);
+        case 5: return build_levels<5, P>(lay, d_values, val_buf, idx_buf, s);
         default: return cudaErrorInvalidValue;
     }
+}
+
+cudaError_t launch_build(const Layout& lay, const float* d_values, float* val_buf,
+                         uint32_t* idx_buf, cudaStream_t s) {
+    return launch_build_p<uint32_t>(lay, d_values, val_buf, idx_buf, s);
+}
+
+cudaError_t launch_build64(const Layout& lay, const float* d_values, float* val_buf,
+                           uint64_t* idx_buf, cudaStream_t s) {
+    return launch_build_p<uint64_t>(lay, d_values, val_buf, idx_buf, s);
 }
 
 }  // namespace rmq

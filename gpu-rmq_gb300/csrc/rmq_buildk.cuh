@@ -11,21 +11,27 @@ constexpr uint32_t kTileSectors = kTile / 8;
 constexpr uint32_t kFusedThreads = 256;
 constexpr uint32_t kTailMaxEntries = 16384;  // largest level the tail CTA reads
 
-struct LevelOut {
+// P: position type (uint32_t, or uint64_t for arrays beyond 2^32 entries).
+template <typename P>
+struct LevelOutT {
     float* val[kMaxLevels];
-    uint32_t* idx[kMaxLevels];  // null entries when argmin arrays are not built
-    uint32_t size[kMaxLevels];
+    P* idx[kMaxLevels];  // null entries when argmin arrays are not built
+    P size[kMaxLevels];
 };
+using LevelOut = LevelOutT<uint32_t>;
 
 // First-occurrence minimum over candidates visited in ascending position;
-// p == kNoPos marks an absent candidate.
-struct VP {
+// p == none marks an absent candidate.
+template <typename P>
+struct VPT {
     float v;
-    uint32_t p;
+    P p;
 };
 
-__device__ __forceinline__ void vp_take(VP& cur, float v, uint32_t p) {
-    if (p != kNoPos && (cur.p == kNoPos || v < cur.v)) {
+template <typename P>
+__device__ __forceinline__ void vp_take(VPT<P>& cur, float v, P p) {
+    constexpr P kNone = IdxTraits<P>::none;
+    if (p != kNone && (cur.p == kNone || v < cur.v)) {
         cur.v = v;
         cur.p = p;
     }
@@ -39,9 +45,11 @@ __host__ __device__ constexpr uint32_t fused_depth() {
 // One CTA of kFusedThreads threads builds levels 1..depth of `tile` (entries
 // [tile * kTile, (tile + 1) * kTile) of level 0); sv / sp are kTileSectors
 // entries of shared memory.
-template <int R>
-__device__ __forceinline__ void fused_tile(const float* __restrict__ a, uint32_t n, const LevelOut& out,
-                                           uint32_t depth, uint32_t tile, float* sv, uint32_t* sp) {
+template <int R, typename P>
+__device__ __forceinline__ void fused_tile(const float* __restrict__ a, P n, const LevelOutT<P>& out,
+                                           uint32_t depth, uint64_t tile, float* sv, P* sp) {
+    using VP = VPT<P>;
+    constexpr P kNone = IdxTraits<P>::none;
     constexpr uint32_t RF = 1u << R;
     constexpr uint32_t SPB = RF / 8u;  // sectors per level-1 block
     const uint32_t tid = threadIdx.x;
@@ -53,7 +61,7 @@ __device__ __forceinline__ void fused_tile(const float* __restrict__ a, uint32_t
     for (uint32_t i = 0; i < kTileSectors / kFusedThreads; ++i) {
         const uint32_t sec = tid + kFusedThreads * i;
         const uint64_t s = base + 8u * sec;
-        VP c{f_inf(), kNoPos};
+        VP c{f_inf(), kNone};
         if (s < n) {
             float v[8];
             if (s + 8u <= n) {
@@ -64,7 +72,7 @@ __device__ __forceinline__ void fused_tile(const float* __restrict__ a, uint32_t
             }
 #pragma unroll
             for (int j = 0; j < 8; ++j)
-                if (s + j < n) vp_take(c, v[j], uint32_t(s + j));
+                if (s + j < n) vp_take(c, v[j], P(s + j));
         }
         sv[sec] = c.v;
         sp[sec] = c.p;
@@ -82,7 +90,7 @@ __device__ __forceinline__ void fused_tile(const float* __restrict__ a, uint32_t
 #pragma unroll
         for (uint32_t i = 0; i < kMaxPer; ++i) {
             const uint32_t e = tid + kFusedThreads * i;
-            res[i] = VP{f_inf(), kNoPos};
+            res[i] = VP{f_inf(), kNone};
             if (e < cnt) {
                 for (uint32_t j = 0; j < fan; ++j) vp_take(res[i], sv[e * fan + j], sp[e * fan + j]);
             }
@@ -110,17 +118,17 @@ __device__ __forceinline__ void fused_tile(const float* __restrict__ a, uint32_t
 // Single CTA: builds levels from+1 .. last from level `from` (already built),
 // level after level, with a block barrier between levels (global writes of
 // the block are visible to it after __syncthreads).
-template <int R>
-__device__ __forceinline__ void tail_levels(const LevelOut& out, uint32_t from, uint32_t last) {
+template <int R, typename P>
+__device__ __forceinline__ void tail_levels(const LevelOutT<P>& out, uint32_t from, uint32_t last) {
     constexpr uint32_t RF = 1u << R;
     for (uint32_t k = from; k < last; ++k) {
         const float* src = out.val[k];
-        const uint32_t* src_idx = out.idx[k];
-        const uint32_t src_size = out.size[k];
-        for (uint32_t e = threadIdx.x; e < out.size[k + 1]; e += blockDim.x) {
-            VP c{f_inf(), kNoPos};
+        const P* src_idx = out.idx[k];
+        const P src_size = out.size[k];
+        for (P e = threadIdx.x; e < out.size[k + 1]; e += blockDim.x) {
+            VPT<P> c{f_inf(), IdxTraits<P>::none};
             for (uint32_t j = 0; j < RF; ++j) {
-                const uint32_t ch = e * RF + j;
+                const P ch = e * RF + j;
                 if (ch < src_size) vp_take(c, src[ch], src_idx != nullptr ? src_idx[ch] : ch);
             }
             out.val[k + 1][e] = c.v;

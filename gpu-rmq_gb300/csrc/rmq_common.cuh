@@ -38,14 +38,33 @@ struct ArrayDesc {
     uint32_t off[kMaxLevels];  // level k >= 1 starts at lvl_base + off[k]
 };
 
+// Index width: 32-bit handles (the reference's default nType = uint32_t,
+// uint2 queries) or 64-bit handles (its IS_LONG build: uint64_t, ulong2
+// queries; src/main.cu:21-27).
+template <typename I>
+struct IdxTraits;
+template <>
+struct IdxTraits<uint32_t> {
+    using Pair = uint2;
+    static constexpr uint32_t none = 0xFFFFFFFFu;
+};
+template <>
+struct IdxTraits<uint64_t> {
+    using Pair = ulonglong2;
+    static constexpr uint64_t none = ~uint64_t(0);
+};
+
 // Device-side view passed by value to the kernels (fits easily in the 32 KB
 // parameter space).
-struct Levels {
-    const float* val[kMaxLevels];      // val[0] = caller's array
-    const uint32_t* idx[kMaxLevels];   // idx[k] (k >= 1): level-0 index of block k's first minimum
-    uint32_t size[kMaxLevels];
+template <typename I>
+struct LevelsT {
+    const float* val[kMaxLevels];  // val[0] = caller's array
+    const I* idx[kMaxLevels];      // idx[k] (k >= 1): level-0 index of block k's first minimum
+    I size[kMaxLevels];
     uint32_t num_levels;
 };
+using Levels = LevelsT<uint32_t>;
+using Levels64 = LevelsT<uint64_t>;
 
 // ---------------------------------------------------------------------------
 // Memory access helpers (inline PTX; sm_100+ 256-bit global loads).  The
@@ -117,6 +136,20 @@ __device__ __forceinline__ uint2 ld_query(const uint2* p) {
     v = __ldg(p);
 #endif
     return v;
+}
+
+__device__ __forceinline__ ulonglong2 ld_query(const ulonglong2* p) {
+    ulonglong2 v;
+    asm(
+        "{\n\t.reg .b64 pol;\n\t"
+        "createpolicy.fractional.L2::evict_first.b64 pol, 1.0;\n\t"
+        "ld.global.nc.L1::no_allocate.L2::cache_hint.v2.u64 {%0,%1}, [%2], pol;\n\t}"
+        : "=l"(v.x), "=l"(v.y) : "l"(p));
+    return v;
+}
+
+__device__ __forceinline__ void st_stream(uint64_t* p, uint64_t v) {
+    asm volatile("st.global.cs.u64 [%0], %1;" :: "l"(p), "l"(v) : "memory");
 }
 
 __device__ __forceinline__ void st_stream(float* p, float v) {

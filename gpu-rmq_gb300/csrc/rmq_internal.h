@@ -17,13 +17,20 @@ Layout plan_layout(uint64_t n, uint64_t t, uint32_t rf_log);
 // `idx_buf` may be null (no argmin support).
 cudaError_t launch_build(const Layout& lay, const float* d_values, float* val_buf,
                          uint32_t* idx_buf, cudaStream_t s);
+// Same with 64-bit positions (arrays beyond 2^32 entries).
+cudaError_t launch_build64(const Layout& lay, const float* d_values, float* val_buf,
+                           uint64_t* idx_buf, cudaStream_t s);
 
 struct QueryArgs {
     Levels lv;
     const uint2* qs;
-    uint32_t q;
+    uint64_t q;
     float* out_min;      // may be null for argmin queries
     uint32_t* out_idx;   // null for min queries
+    bool wide;           // 64-bit positions: lv64 / qs64 / out_idx64 are used instead
+    Levels64 lv64;
+    const uint64_t* qs64;
+    uint64_t* out_idx64;
     uint32_t* err;       // invalid-query counter or null
     int variant;         // 1 = CL, 2 = VL
     int lanes;           // CL tile width

@@ -85,7 +85,7 @@ extern "C" int rmq_query_idx_static(const float* d_values, uint64_t n, uint64_t 
         }
         a.lv.num_levels = lay.num_levels;
         a.qs = reinterpret_cast<const uint2*>(d_lr);
-        a.q = uint32_t(q);
+        a.q = q;
         a.out_min = d_min_or_null;
         a.out_idx = d_argmin;
         a.variant = RMQ_VARIANT_VL;

@@ -19,12 +19,12 @@
 
 namespace rmq {
 
-template <int R, bool ARGMIN>
+template <int R, bool ARGMIN, typename I>
 __global__ void __launch_bounds__(256)
-query_vl_kernel(Levels lv, const uint2* __restrict__ qs, uint32_t q, float* __restrict__ out_min,
-                uint32_t* __restrict__ out_idx, uint32_t* __restrict__ err) {
+query_vl_kernel(LevelsT<I> lv, const typename IdxTraits<I>::Pair* __restrict__ qs, uint64_t q,
+                float* __restrict__ out_min, I* __restrict__ out_idx, uint32_t* __restrict__ err) {
     // No early return: every lane takes part in the warp's long final scans.
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     vl_answer<R, ARGMIN>(lv, qs, i, i < q, out_min, out_idx, err);
 }
 
@@ -239,8 +239,9 @@ bruteforce_kernel(const float* __restrict__ a, uint32_t n, const uint2* __restri
 // Launchers
 // ---------------------------------------------------------------------------
 
-template <typename K>
-static cudaError_t launch_with_window(K kernel, uint32_t grid, const QueryArgs& a, cudaStream_t s) {
+template <typename K, typename... Args>
+static cudaError_t launch_with_window(K kernel, uint32_t grid, const QueryArgs& a, cudaStream_t s,
+                                      Args... args) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
     cfg.blockDim = dim3(256);
@@ -260,34 +261,42 @@ static cudaError_t launch_with_window(K kernel, uint32_t grid, const QueryArgs& 
         cfg.attrs = nullptr;
         cfg.numAttrs = 0;
     }
-    return cudaLaunchKernelEx(&cfg, kernel, a.lv, a.qs, a.q, a.out_min, a.out_idx, a.err);
+    return cudaLaunchKernelEx(&cfg, kernel, args...);
 }
 
 template <int R>
 static cudaError_t launch_query_r(const QueryArgs& a, cudaStream_t s) {
-    const bool argmin = a.out_idx != nullptr;
+    const bool argmin = a.out_idx != nullptr || a.out_idx64 != nullptr;
+    const uint32_t grid = uint32_t((a.q + 255u) / 256u);
+    if (a.wide) {
+        // 64-bit positions: the VL kernel only.
+        if (a.variant != 2) return cudaErrorNotSupported;
+        const ulonglong2* qs = reinterpret_cast<const ulonglong2*>(a.qs64);
+        return argmin ? launch_with_window(query_vl_kernel<R, true, uint64_t>, grid, a, s, a.lv64, qs, a.q,
+                                           a.out_min, a.out_idx64, a.err)
+                      : launch_with_window(query_vl_kernel<R, false, uint64_t>, grid, a, s, a.lv64, qs, a.q,
+                                           a.out_min, static_cast<uint64_t*>(nullptr), a.err);
+    }
     if (a.variant == 2) {
-        const uint32_t grid = (a.q + 255u) / 256u;
-        return argmin ? launch_with_window(query_vl_kernel<R, true>, grid, a, s)
-                      : launch_with_window(query_vl_kernel<R, false>, grid, a, s);
+        return argmin ? launch_with_window(query_vl_kernel<R, true, uint32_t>, grid, a, s, a.lv, a.qs, a.q,
+                                           a.out_min, a.out_idx, a.err)
+                      : launch_with_window(query_vl_kernel<R, false, uint32_t>, grid, a, s, a.lv, a.qs, a.q,
+                                           a.out_min, static_cast<uint32_t*>(nullptr), a.err);
     }
-    const uint32_t grid = (a.q + 255u) / 256u;
+    const uint32_t q32 = uint32_t(a.q);
+#define RMQ_CL(G)                                                                                            \
+    return argmin ? launch_with_window(query_cl_kernel<R, G, true>, grid, a, s, a.lv, a.qs, q32, a.out_min,  \
+                                       a.out_idx, a.err)                                                     \
+                  : launch_with_window(query_cl_kernel<R, G, false>, grid, a, s, a.lv, a.qs, q32, a.out_min, \
+                                       static_cast<uint32_t*>(nullptr), a.err)
     switch (a.lanes) {
-        case 4:
-            return argmin ? launch_with_window(query_cl_kernel<R, 4, true>, grid, a, s)
-                          : launch_with_window(query_cl_kernel<R, 4, false>, grid, a, s);
-        case 8:
-            return argmin ? launch_with_window(query_cl_kernel<R, 8, true>, grid, a, s)
-                          : launch_with_window(query_cl_kernel<R, 8, false>, grid, a, s);
-        case 16:
-            return argmin ? launch_with_window(query_cl_kernel<R, 16, true>, grid, a, s)
-                          : launch_with_window(query_cl_kernel<R, 16, false>, grid, a, s);
-        case 32:
-            return argmin ? launch_with_window(query_cl_kernel<R, 32, true>, grid, a, s)
-                          : launch_with_window(query_cl_kernel<R, 32, false>, grid, a, s);
-        default:
-            return cudaErrorInvalidValue;
+        case 4: RMQ_CL(4);
+        case 8: RMQ_CL(8);
+        case 16: RMQ_CL(16);
+        case 32: RMQ_CL(32);
+        default: return cudaErrorInvalidValue;
     }
+#undef RMQ_CL
 }
 
 cudaError_t launch_query(const QueryArgs& a, cudaStream_t s) {

@@ -60,9 +60,23 @@ __device__ __forceinline__ uint32_t ld_index(const uint32_t* p) {
 #endif
 }
 
+__device__ __forceinline__ uint64_t ld_index(const uint64_t* p) {
+#if RMQ_IDX_HINT == 0
+    uint64_t v;
+    asm("{\n\t.reg .b64 pol;\n\t"
+        "createpolicy.fractional.L2::evict_last.b64 pol, 1.0;\n\t"
+        "ld.global.nc.L2::cache_hint.u64 %0, [%1], pol;\n\t}"
+        : "=l"(v) : "l"(p));
+    return v;
+#else
+    return __ldg(reinterpret_cast<const unsigned long long*>(p));
+#endif
+}
+
 // Loads the sector starting at s of level k.  Level 0 is the caller's array,
 // which is not padded: a sector that crosses its end is read element-wise.
-__device__ __forceinline__ void load_level_sector(const Levels& lv, uint32_t k, uint32_t s,
+template <typename I>
+__device__ __forceinline__ void load_level_sector(const LevelsT<I>& lv, uint32_t k, I s,
                                                   const L2Policies& pol, float (&v)[8]) {
     const float* base = lv.val[k];
     if (k > 0) {
@@ -70,9 +84,9 @@ __device__ __forceinline__ void load_level_sector(const Levels& lv, uint32_t k, 
     } else if (s + 8u <= lv.size[0]) {
         ld_sector_policy(base + s, v, pol.fine);
     } else {
-        const uint32_t size = lv.size[0];
+        const I size = lv.size[0];
 #pragma unroll
-        for (int j = 0; j < 8; ++j) v[j] = (s + j < size) ? base[s + j] : f_inf();
+        for (int j = 0; j < 8; ++j) v[j] = (s + I(j) < size) ? base[s + j] : f_inf();
     }
 }
 
@@ -88,21 +102,23 @@ __device__ __forceinline__ float sector_min(const float (&v)[8], uint32_t jlo, u
 
 // Sector-granular position of the first minimum.  meta packs the level
 // (bits 0-7), jlo (bits 8-15) and jhi (bits 16-23); kNoPos = none yet.
+template <typename I>
 struct Tracker {
     float v;
-    uint32_t s;
+    I s;
     uint32_t meta;
 };
 
-__device__ __forceinline__ void tracker_init(Tracker& t) {
+template <typename I>
+__device__ __forceinline__ void tracker_init(Tracker<I>& t) {
     t.v = f_inf();
     t.s = 0;
     t.meta = kNoPos;
 }
 
-template <bool ARGMIN, bool RIGHT>
-__device__ __forceinline__ void scan_sector(const Levels& lv, uint32_t k, uint32_t s, uint32_t jlo,
-                                            uint32_t jhi, const L2Policies& pol, float& m, Tracker& t) {
+template <bool ARGMIN, bool RIGHT, typename I>
+__device__ __forceinline__ void scan_sector(const LevelsT<I>& lv, uint32_t k, I s, uint32_t jlo,
+                                            uint32_t jhi, const L2Policies& pol, float& m, Tracker<I>& t) {
     float v[8];
     load_level_sector(lv, k, s, pol, v);
     const float sm = sector_min(v, jlo, jhi);
@@ -118,24 +134,24 @@ __device__ __forceinline__ void scan_sector(const Levels& lv, uint32_t k, uint32
 }
 
 // Ascending scan of [lo, hi) (lo < hi) at level k, sector by sector.
-template <bool ARGMIN>
-__device__ __forceinline__ void scan_fwd(const Levels& lv, uint32_t k, uint32_t lo, uint32_t hi,
-                                         const L2Policies& pol, float& m, Tracker& t) {
-    for (uint32_t s = lo & ~7u; s < hi; s += 8u) {
-        const uint32_t jlo = s < lo ? lo - s : 0u;
-        const uint32_t jhi = hi - s < 8u ? hi - s : 8u;
+template <bool ARGMIN, typename I>
+__device__ __forceinline__ void scan_fwd(const LevelsT<I>& lv, uint32_t k, I lo, I hi,
+                                         const L2Policies& pol, float& m, Tracker<I>& t) {
+    for (I s = lo & ~I(7); s < hi; s += 8u) {
+        const uint32_t jlo = s < lo ? uint32_t(lo - s) : 0u;
+        const uint32_t jhi = hi - s < 8u ? uint32_t(hi - s) : 8u;
         scan_sector<ARGMIN, false>(lv, k, s, jlo, jhi, pol, m, t);
     }
 }
 
 // Descending scan of [lo, hi) (lo < hi) at level k (right pieces).
-template <bool ARGMIN>
-__device__ __forceinline__ void scan_bwd(const Levels& lv, uint32_t k, uint32_t lo, uint32_t hi,
-                                         const L2Policies& pol, float& m, Tracker& t) {
-    const uint32_t first = lo & ~7u;
-    for (uint32_t s = (hi - 1u) & ~7u;; s -= 8u) {
-        const uint32_t jlo = s < lo ? lo - s : 0u;
-        const uint32_t jhi = hi - s < 8u ? hi - s : 8u;
+template <bool ARGMIN, typename I>
+__device__ __forceinline__ void scan_bwd(const LevelsT<I>& lv, uint32_t k, I lo, I hi,
+                                         const L2Policies& pol, float& m, Tracker<I>& t) {
+    const I first = lo & ~I(7);
+    for (I s = (hi - 1u) & ~I(7);; s -= 8u) {
+        const uint32_t jlo = s < lo ? uint32_t(lo - s) : 0u;
+        const uint32_t jhi = hi - s < 8u ? uint32_t(hi - s) : 8u;
         scan_sector<ARGMIN, true>(lv, k, s, jlo, jhi, pol, m, t);
         if (s == first) break;
     }
@@ -147,37 +163,38 @@ constexpr uint32_t kLongScan = 64;
 
 // Phase 1 up to (not including) the final piece; returns the running minimum
 // and leaves the final piece [l, r) at level k in the arguments.
-template <int R, bool ARGMIN>
-__device__ __forceinline__ float vl_descend(const Levels& lv, uint32_t& l, uint32_t& r, uint32_t& k,
-                                            const L2Policies& pol, Tracker& tl, Tracker& tr) {
-    constexpr uint32_t RF = 1u << R;
+template <int R, bool ARGMIN, typename I>
+__device__ __forceinline__ float vl_descend(const LevelsT<I>& lv, I& l, I& r, uint32_t& k,
+                                            const L2Policies& pol, Tracker<I>& tl, Tracker<I>& tr) {
+    constexpr I RF = I(1) << R;
     float m = f_inf();
     k = 0;
     while (k + 1 < lv.num_levels && r - l > 2u * RF) {
-        const uint32_t nl = (l + RF - 1) & ~(RF - 1);
-        const uint32_t pr = r & ~(RF - 1);
+        const I nl = (l + RF - 1) & ~(RF - 1);
+        const I pr = r & ~(RF - 1);
         if (R == 3) {
             // rf = 8: each boundary piece is exactly one sector; issue both loads first.
             float a[8], b[8];
             const bool has_l = nl > l, has_r = r > pr;
-            if (has_l) load_level_sector(lv, k, l & ~7u, pol, a);
+            const uint32_t lo_j = uint32_t(l & 7u), hi_j = uint32_t(r - pr);
+            if (has_l) load_level_sector(lv, k, l & ~I(7), pol, a);
             if (has_r) load_level_sector(lv, k, pr, pol, b);
             if (has_l) {
-                const float sm = sector_min(a, l & 7u, 8u);
+                const float sm = sector_min(a, lo_j, 8u);
                 m = fminf(m, sm);
                 if (ARGMIN && sm < tl.v) {
                     tl.v = sm;
-                    tl.s = l & ~7u;
-                    tl.meta = k | ((l & 7u) << 8) | (8u << 16);
+                    tl.s = l & ~I(7);
+                    tl.meta = k | (lo_j << 8) | (8u << 16);
                 }
             }
             if (has_r) {
-                const float sm = sector_min(b, 0u, r - pr);
+                const float sm = sector_min(b, 0u, hi_j);
                 m = fminf(m, sm);
                 if (ARGMIN && sm <= tr.v) {
                     tr.v = sm;
                     tr.s = pr;
-                    tr.meta = k | ((r - pr) << 16);
+                    tr.meta = k | (hi_j << 16);
                 }
             }
         } else {
@@ -196,19 +213,20 @@ __device__ __forceinline__ float vl_descend(const Levels& lv, uint32_t& l, uint3
 // per warp load), keeps its first sector holding its minimum, and the warp
 // combines by (value, sector start) so the first sector holding the piece
 // minimum wins; the owner merges it into its running minimum and tracker.
-template <bool ARGMIN>
-__device__ __forceinline__ void warp_scan_final(const Levels& lv, uint32_t k, uint32_t lo, uint32_t hi,
-                                                uint32_t owner, const L2Policies& pol, float& m, Tracker& tl) {
+template <bool ARGMIN, typename I>
+__device__ __forceinline__ void warp_scan_final(const LevelsT<I>& lv, uint32_t k, I lo, I hi,
+                                                uint32_t owner, const L2Policies& pol, float& m, Tracker<I>& tl) {
+    constexpr I kNone = IdxTraits<I>::none;
     const uint32_t lane = threadIdx.x & 31u;
     float best = f_inf();
-    uint32_t bs = kNoPos;
-    for (uint32_t s = (lo & ~7u) + 8u * lane; s < hi; s += 256u) {
-        const uint32_t jlo = s < lo ? lo - s : 0u;
-        const uint32_t jhi = hi - s < 8u ? hi - s : 8u;
+    I bs = kNone;
+    for (I s = (lo & ~I(7)) + 8u * lane; s < hi; s += 256u) {
+        const uint32_t jlo = s < lo ? uint32_t(lo - s) : 0u;
+        const uint32_t jhi = hi - s < 8u ? uint32_t(hi - s) : 8u;
         float v[8];
         load_level_sector(lv, k, s, pol, v);
         const float sm = sector_min(v, jlo, jhi);
-        if (bs == kNoPos || sm < best) {
+        if (bs == kNone || sm < best) {
             best = sm;
             bs = s;
         }
@@ -216,8 +234,8 @@ __device__ __forceinline__ void warp_scan_final(const Levels& lv, uint32_t k, ui
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         const float ov = __shfl_xor_sync(0xffffffffu, best, o);
-        const uint32_t os = __shfl_xor_sync(0xffffffffu, bs, o);
-        if (os != kNoPos && (bs == kNoPos || ov < best || (ov == best && os < bs))) {
+        const I os = __shfl_xor_sync(0xffffffffu, bs, o);
+        if (os != kNone && (bs == kNone || ov < best || (ov == best && os < bs))) {
             best = ov;
             bs = os;
         }
@@ -227,8 +245,8 @@ __device__ __forceinline__ void warp_scan_final(const Levels& lv, uint32_t k, ui
         if (ARGMIN && best < tl.v) {
             tl.v = best;
             tl.s = bs;
-            const uint32_t jlo = bs < lo ? lo - bs : 0u;
-            const uint32_t jhi = hi - bs < 8u ? hi - bs : 8u;
+            const uint32_t jlo = bs < lo ? uint32_t(lo - bs) : 0u;
+            const uint32_t jhi = hi - bs < 8u ? uint32_t(hi - bs) : 8u;
             tl.meta = k | (jlo << 8) | (jhi << 16);
         }
     }
@@ -236,9 +254,9 @@ __device__ __forceinline__ void warp_scan_final(const Levels& lv, uint32_t k, ui
 
 // Phase 1 for every lane of the warp (all 32 lanes must call it): private
 // descent and short final scans, then the warp's long final scans one by one.
-template <int R, bool ARGMIN>
-__device__ __forceinline__ float vl_phase1(const Levels& lv, bool active, uint32_t l, uint32_t r,
-                                           const L2Policies& pol, Tracker& tl, Tracker& tr) {
+template <int R, bool ARGMIN, typename I>
+__device__ __forceinline__ float vl_phase1(const LevelsT<I>& lv, bool active, I l, I r,
+                                           const L2Policies& pol, Tracker<I>& tl, Tracker<I>& tr) {
     float m = f_inf();
     uint32_t k = 0;
     bool is_long = false;
@@ -251,8 +269,8 @@ __device__ __forceinline__ float vl_phase1(const Levels& lv, bool active, uint32
     while (pending != 0u) {
         const uint32_t owner = uint32_t(__ffs(pending) - 1);
         const uint32_t ok = __shfl_sync(0xffffffffu, k, owner);
-        const uint32_t olo = __shfl_sync(0xffffffffu, l, owner);
-        const uint32_t ohi = __shfl_sync(0xffffffffu, r, owner);
+        const I olo = __shfl_sync(0xffffffffu, l, owner);
+        const I ohi = __shfl_sync(0xffffffffu, r, owner);
         warp_scan_final<ARGMIN>(lv, ok, olo, ohi, owner, pol, m, tl);
         pending &= pending - 1u;
     }
@@ -260,11 +278,11 @@ __device__ __forceinline__ float vl_phase1(const Levels& lv, bool active, uint32
 }
 
 // Phase 2: first entry equal to the minimum inside the winning sector.
-template <int R>
-__device__ __forceinline__ void vl_locate(const Levels& lv, uint32_t l, const Tracker& tl, const Tracker& tr,
-                                          const L2Policies& pol, float& out_v, uint32_t& out_i) {
+template <int R, typename I>
+__device__ __forceinline__ void vl_locate(const LevelsT<I>& lv, I l, const Tracker<I>& tl, const Tracker<I>& tr,
+                                          const L2Policies& pol, float& out_v, I& out_i) {
     const bool right = tr.v < tl.v;
-    const Tracker& w = right ? tr : tl;
+    const Tracker<I>& w = right ? tr : tl;
     if (w.meta == kNoPos) {
         // No candidate compared below +inf: every entry is +inf (or NaN,
         // outside the contract); the scan's answer is the first entry.
@@ -285,7 +303,7 @@ __device__ __forceinline__ void vl_locate(const Levels& lv, uint32_t l, const Tr
     float val = v[0];
 #pragma unroll
     for (int jj = 1; jj < 8; ++jj) val = (uint32_t(jj) == j) ? v[jj] : val;
-    const uint32_t e = w.s + j;
+    const I e = w.s + j;
     out_v = val;
     out_i = k == 0 ? e : ld_index(lv.idx[k] + e);
 }
@@ -294,15 +312,16 @@ __device__ __forceinline__ void vl_locate(const Levels& lv, uint32_t l, const Tr
 // it (long final scans are shared by the warp).  For a valid query
 // (0 <= l <= r < n) returns true with the minimum in v and, for ARGMIN, the
 // argmin in idx; an invalid or absent (active = false) query returns false.
-template <int R, bool ARGMIN>
-__device__ __forceinline__ bool vl_compute(const Levels& lv, uint2 Q, bool active, float& v, uint32_t& idx) {
+template <int R, bool ARGMIN, typename I>
+__device__ __forceinline__ bool vl_compute(const LevelsT<I>& lv, typename IdxTraits<I>::Pair Q, bool active,
+                                           float& v, I& idx) {
     const bool valid = active && Q.x <= Q.y && Q.y < lv.size[0];
     const L2Policies pol = make_policies();
-    const uint32_t l = Q.x, r = Q.y + 1;
-    Tracker tl, tr;
+    const I l = Q.x, r = Q.y + 1;
+    Tracker<I> tl, tr;
     tracker_init(tl);
     tracker_init(tr);
-    idx = kNoPos;
+    idx = IdxTraits<I>::none;
     if (ARGMIN) {
         vl_phase1<R, true>(lv, valid, l, r, pol, tl, tr);
         v = f_nan();
@@ -323,9 +342,9 @@ __device__ __forceinline__ bool vl_compute(const Levels& lv, uint2 Q, bool activ
 
 // Stores of one answered query: NaN / kNoPos for an invalid query, which is
 // also counted in *err when err is given.
-template <bool ARGMIN>
-__device__ __forceinline__ void vl_store(bool in_range, bool valid, float v, uint32_t idx, float* out_min,
-                                         uint32_t* out_idx, uint32_t* err) {
+template <bool ARGMIN, typename I>
+__device__ __forceinline__ void vl_store(bool in_range, bool valid, float v, I idx, float* out_min,
+                                         I* out_idx, uint32_t* err) {
     if (!in_range) return;
     if (out_min != nullptr) st_stream(out_min, v);
     if (ARGMIN) st_stream(out_idx, idx);
@@ -334,14 +353,16 @@ __device__ __forceinline__ void vl_store(bool in_range, bool valid, float v, uin
 
 // Query i of qs (when in_range) into out_min[i] / out_idx[i]; every lane of
 // the warp must call it.
-template <int R, bool ARGMIN>
-__device__ __forceinline__ void vl_answer(const Levels& lv, const uint2* __restrict__ qs, uint32_t i,
-                                          bool in_range, float* __restrict__ out_min,
-                                          uint32_t* __restrict__ out_idx, uint32_t* __restrict__ err) {
-    uint2 Q = make_uint2(1u, 0u);
+template <int R, bool ARGMIN, typename I>
+__device__ __forceinline__ void vl_answer(const LevelsT<I>& lv, const typename IdxTraits<I>::Pair* __restrict__ qs,
+                                          uint64_t i, bool in_range, float* __restrict__ out_min,
+                                          I* __restrict__ out_idx, uint32_t* __restrict__ err) {
+    typename IdxTraits<I>::Pair Q;
+    Q.x = 1u;
+    Q.y = 0u;
     if (in_range) Q = ld_query(qs + i);
     float v;
-    uint32_t idx;
+    I idx;
     const bool valid = vl_compute<R, ARGMIN>(lv, Q, in_range, v, idx);
     vl_store<ARGMIN>(in_range, valid, v, idx, out_min != nullptr ? out_min + i : nullptr,
                      ARGMIN ? out_idx + i : nullptr, err);

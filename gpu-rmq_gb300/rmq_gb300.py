@@ -53,6 +53,7 @@ class RMQConfig(ctypes.Structure):
         ("with_index", ctypes.c_int32),
         ("l2_persist", ctypes.c_int32),
         ("validate", ctypes.c_int32),
+        ("index_bits", ctypes.c_int32),
     ]
 
 
@@ -68,6 +69,7 @@ class RMQInfo(ctypes.Structure):
         ("level_offset", ctypes.c_uint64 * 20),
         ("level_bytes", ctypes.c_uint64),
         ("build_ms", ctypes.c_float),
+        ("index_bits", ctypes.c_int32),
     ]
 
     def sizes(self) -> list[int]:
@@ -105,6 +107,10 @@ def lib() -> ctypes.CDLL:
         L.rmq_query.restype = ctypes.c_int
         L.rmq_query_idx.argtypes = [_P, _P, _U64, _P, _P, _P]
         L.rmq_query_idx.restype = ctypes.c_int
+        L.rmq_query64.argtypes = [_P, _P, _U64, _P, _P]
+        L.rmq_query64.restype = ctypes.c_int
+        L.rmq_query_idx64.argtypes = [_P, _P, _U64, _P, _P, _P]
+        L.rmq_query_idx64.restype = ctypes.c_int
         L.rmq_scan_bruteforce.argtypes = [_P, _U64, _P, _U64, _P, _P, _P]
         L.rmq_scan_bruteforce.restype = ctypes.c_int
         L.rmq_get_info.argtypes = [_P, ctypes.POINTER(RMQInfo)]
@@ -142,7 +148,8 @@ def strerror(status: int) -> str:
 
 
 def config(variant: str | int = "auto", t: int = 0, rf_log: int = 0, lanes: int = 0,
-           with_index: bool = True, l2_persist: bool = False, validate: bool = False) -> RMQConfig:
+           with_index: bool = True, l2_persist: bool = False, validate: bool = False,
+           index_bits: int = 0) -> RMQConfig:
     cfg = RMQConfig()
     lib().rmq_config_init(ctypes.byref(cfg))
     cfg.variant = VARIANTS[variant] if isinstance(variant, str) else int(variant)
@@ -152,6 +159,7 @@ def config(variant: str | int = "auto", t: int = 0, rf_log: int = 0, lanes: int 
     cfg.with_index = 1 if with_index else 0
     cfg.l2_persist = 1 if l2_persist else 0
     cfg.validate = 1 if validate else 0
+    cfg.index_bits = int(index_bits)
     return cfg
 
 
@@ -183,7 +191,7 @@ class Hierarchy:
 
     def __init__(self, values, variant: str | int = "auto", t: int = 0, rf_log: int = 0,
                  lanes: int = 0, with_index: bool = True, l2_persist: bool = False,
-                 validate: bool = False, stream=None):
+                 validate: bool = False, stream=None, index_bits: int = 0):
         import torch
         if not isinstance(values, torch.Tensor) or values.device.type != "cuda":
             raise TypeError("values must be a CUDA torch tensor")
@@ -191,7 +199,7 @@ class Hierarchy:
             raise TypeError("values must be contiguous float32")
         self.values = values  # level 0 is the caller's array: keep it alive
         self.n = values.numel()
-        cfg = config(variant, t, rf_log, lanes, with_index, l2_persist, validate)
+        cfg = config(variant, t, rf_log, lanes, with_index, l2_persist, validate, index_bits)
         h = _P()
         st = lib().rmq_build(_dev_ptr(values), self.n, ctypes.byref(cfg), _stream_handle(stream),
                              ctypes.byref(h))
@@ -240,6 +248,29 @@ class Hierarchy:
                                 _dev_ptr(out_min) if out_min is not None else None, stream)
         if st != RMQ_OK:
             raise RMQError(st, "rmq_query_idx")
+        return (out_idx, out_min) if with_min else out_idx
+
+    def query64(self, lr, out=None, stream=None):
+        """Minima of 64-bit inclusive queries (CUDA int64 tensor [q, 2]); 64-bit handles."""
+        import torch
+        q = lr.numel() // 2
+        if out is None:
+            out = torch.empty(q, dtype=torch.float32, device=lr.device)
+        st = lib().rmq_query64(self._h, _dev_ptr(lr), q, _dev_ptr(out), _stream_handle(stream))
+        if st != RMQ_OK:
+            raise RMQError(st, "rmq_query64")
+        return out
+
+    def query_idx64(self, lr, with_min: bool = False, stream=None):
+        """Argmin (int64 tensor) and optionally minima of 64-bit queries."""
+        import torch
+        q = lr.numel() // 2
+        out_idx = torch.empty(q, dtype=torch.int64, device=lr.device)
+        out_min = torch.empty(q, dtype=torch.float32, device=lr.device) if with_min else None
+        st = lib().rmq_query_idx64(self._h, _dev_ptr(lr), q, _dev_ptr(out_idx),
+                                   _dev_ptr(out_min) if out_min is not None else None, _stream_handle(stream))
+        if st != RMQ_OK:
+            raise RMQError(st, "rmq_query_idx64")
         return (out_idx, out_min) if with_min else out_idx
 
     def close(self) -> None:

@@ -12,8 +12,9 @@
  *                  (IEEE-754 "<", so ties, including -0.0 vs +0.0, go to the
  *                  lowest index).
  * Inputs holding NaN are outside the contract.  A query with l > r or r >= n
- * is invalid: its min is written as NaN and its argmin as 0xFFFFFFFF, and with
- * cfg.validate set the call reports RMQ_ERR_QUERY_RANGE.
+ * is invalid: its min is written as NaN and its argmin as all ones
+ * (0xFFFFFFFF, or 2^64 - 1 for 64-bit queries), and with cfg.validate set the
+ * call reports RMQ_ERR_QUERY_RANGE.
  *
  * No entry point exits the process or traps the GPU; all return a status.
  * rmq_query / rmq_query_idx do not allocate, do not synchronise (unless
@@ -59,6 +60,7 @@ typedef struct {
     int32_t  with_index;      /* build the per-block argmin arrays (needed by rmq_query_idx)             */
     int32_t  l2_persist;      /* put the coarse levels in an L2 persisting access-policy window          */
     int32_t  validate;        /* count invalid queries on the device; query calls then synchronise       */
+    int32_t  index_bits;      /* 32 or 64 (0 = 32, or 64 when n > 0xFFFFFF00); 64 = rmq_query*64 only, VL   */
 } rmq_config;
 
 typedef struct {
@@ -72,6 +74,7 @@ typedef struct {
     uint64_t level_offset[20];  /* element offset of level k >= 1 in the level buffer    */
     uint64_t level_bytes;       /* device bytes of level values (+ argmin arrays)        */
     float    build_ms;          /* device time of the last build (CUDA events)           */
+    int32_t  index_bits;        /* 32 or 64                                              */
 } rmq_info;
 
 /* Fills *cfg with the defaults: AUTO variant, default t and rf, with_index = 1,
@@ -99,6 +102,17 @@ int rmq_query(const rmq_handle* h, const uint32_t* d_lr, uint64_t q, float* d_mi
  * cpu_rmq_idx (src/cpu_methods.h:56). */
 int rmq_query_idx(const rmq_handle* h, const uint32_t* d_lr, uint64_t q,
                   uint32_t* d_argmin, float* d_min_or_null, rmq_stream_t stream);
+
+/* 64-bit counterparts for handles built with index_bits = 64 (the
+ * reference's IS_LONG build: uint64_t indices and ulong2 queries,
+ * src/main.cu:21-27, for arrays beyond 2^32 entries): d_lr holds q inclusive
+ * pairs of uint64 {l, r}; argmin results are uint64.  Same semantics; the VL
+ * work distribution.  A 32-bit handle returns RMQ_ERR_UNSUPPORTED here, and a
+ * 64-bit handle does so from rmq_query / rmq_query_idx. */
+int rmq_query64(const rmq_handle* h, const uint64_t* d_lr, uint64_t q, float* d_min,
+                rmq_stream_t stream);
+int rmq_query_idx64(const rmq_handle* h, const uint64_t* d_lr, uint64_t q, uint64_t* d_argmin,
+                    float* d_min_or_null, rmq_stream_t stream);
 
 /* Brute-force scan, one thread per query (the reference's GPU checker,
  * kernel_rmq_basic / kernel_rmq_basic_idx, src/cuda_methods.cuh:4-44).

@@ -75,8 +75,11 @@ def test_plan_layout_defaults_and_preconditions():
     R.plan_layout(1 << 20, 8, 3, "vl")
     with pytest.raises(R.RMQError):
         R.plan_layout(1 << 20, 64, 6, "vl")
+    wide = R.plan_layout(1 << 33, 64, 3, "vl")  # beyond 32-bit indices: a 64-bit layout
+    assert wide.index_bits == 64 and wide.sizes()[1] == 1 << 30
+    assert R.plan_layout(1 << 20, 64, 3, "vl").index_bits == 32
     with pytest.raises(R.RMQError) as e:
-        R.plan_layout(1 << 33, 64, 3, "vl")
+        R.plan_layout((1 << 40) + 1, 64, 3, "vl")
     assert e.value.status == R.RMQ_ERR_UNSUPPORTED
 
 
