@@ -24,7 +24,8 @@ __global__ void __launch_bounds__(256)
 query_vl_kernel(LevelsT<I> lv, const typename IdxTraits<I>::Pair* __restrict__ qs, uint64_t q,
                 float* __restrict__ out_min, I* __restrict__ out_idx, uint32_t* __restrict__ err) {
     // No early return: every lane takes part in the warp's long final scans.
-    const uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    using C = typename IdxTraits<I>::Count;
+    const C i = C(blockIdx.x) * blockDim.x + threadIdx.x;
     vl_answer<R, ARGMIN>(lv, qs, i, i < q, out_min, out_idx, err);
 }
 

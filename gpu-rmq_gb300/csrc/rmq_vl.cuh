@@ -17,7 +17,7 @@ namespace rmq {
 // first), right pieces in descending order ("<=" lets the more-left sector
 // win), and a left/final winner beats a right winner on equal values.
 // Phase 2 re-reads only the winning sector, takes its first entry equal to the
-// minimum and, for a coarse level, loads that entry's stored level-0 index.
+// minimum and, for a coarse level, that entry's stored level-0 index.
 // ---------------------------------------------------------------------------
 
 // L2 eviction priorities (tuning knobs; 0 selects the default shown).
@@ -277,7 +277,10 @@ __device__ __forceinline__ float vl_phase1(const LevelsT<I>& lv, bool active, I 
     return m;
 }
 
-// Phase 2: first entry equal to the minimum inside the winning sector.
+// Phase 2: first entry equal to the minimum inside the winning sector.  For
+// a coarse winner of a 32-bit handle the sector's eight stored level-0
+// indices (one 32-byte sector, level offsets are 32-entry aligned) are loaded
+// together with its values, so the index needs no further round trip.
 template <int R, typename I>
 __device__ __forceinline__ void vl_locate(const LevelsT<I>& lv, I l, const Tracker<I>& tl, const Tracker<I>& tr,
                                           const L2Policies& pol, float& out_v, I& out_i) {
@@ -295,6 +298,10 @@ __device__ __forceinline__ void vl_locate(const LevelsT<I>& lv, I l, const Track
     const uint32_t jhi = (w.meta >> 16) & 0xffu;
     float v[8];
     load_level_sector(lv, k, w.s, pol, v);
+    uint32_t ix[8];
+    if constexpr (sizeof(I) == 4) {
+        if (k > 0) ld_sector_u32_policy(lv.idx[k] + w.s, ix, pol.coarse);
+    }
     uint32_t j = jlo;
 #pragma unroll
     for (int jj = 7; jj >= 0; --jj) {
@@ -305,7 +312,14 @@ __device__ __forceinline__ void vl_locate(const LevelsT<I>& lv, I l, const Track
     for (int jj = 1; jj < 8; ++jj) val = (uint32_t(jj) == j) ? v[jj] : val;
     const I e = w.s + j;
     out_v = val;
-    out_i = k == 0 ? e : ld_index(lv.idx[k] + e);
+    if constexpr (sizeof(I) == 4) {
+        uint32_t x = ix[0];
+#pragma unroll
+        for (int jj = 1; jj < 8; ++jj) x = (uint32_t(jj) == j) ? ix[jj] : x;
+        out_i = k == 0 ? e : x;
+    } else {
+        out_i = k == 0 ? e : ld_index(lv.idx[k] + e);
+    }
 }
 
 // One query per thread, no memory writes: every lane of the warp must call
@@ -355,7 +369,7 @@ __device__ __forceinline__ void vl_store(bool in_range, bool valid, float v, I i
 // the warp must call it.
 template <int R, bool ARGMIN, typename I>
 __device__ __forceinline__ void vl_answer(const LevelsT<I>& lv, const typename IdxTraits<I>::Pair* __restrict__ qs,
-                                          uint64_t i, bool in_range, float* __restrict__ out_min,
+                                          typename IdxTraits<I>::Count i, bool in_range, float* __restrict__ out_min,
                                           I* __restrict__ out_idx, uint32_t* __restrict__ err) {
     typename IdxTraits<I>::Pair Q;
     Q.x = 1u;
