@@ -116,11 +116,11 @@ __device__ __forceinline__ void tracker_init(Tracker<I>& t) {
     t.meta = kNoPos;
 }
 
+// Folds the loaded sector v (start s of level k, entries [jlo, jhi)) into
+// the running minimum and the side's candidate.
 template <bool ARGMIN, bool RIGHT, typename I>
-__device__ __forceinline__ void scan_sector(const LevelsT<I>& lv, uint32_t k, I s, uint32_t jlo,
-                                            uint32_t jhi, const L2Policies& pol, float& m, Tracker<I>& t) {
-    float v[8];
-    load_level_sector(lv, k, s, pol, v);
+__device__ __forceinline__ void take_sector(const float (&v)[8], uint32_t k, I s, uint32_t jlo, uint32_t jhi,
+                                            float& m, Tracker<I>& t) {
     const float sm = sector_min(v, jlo, jhi);
     m = fminf(m, sm);
     if (ARGMIN) {
@@ -133,11 +133,30 @@ __device__ __forceinline__ void scan_sector(const LevelsT<I>& lv, uint32_t k, I 
     }
 }
 
-// Ascending scan of [lo, hi) (lo < hi) at level k, sector by sector.
+template <bool ARGMIN, bool RIGHT, typename I>
+__device__ __forceinline__ void scan_sector(const LevelsT<I>& lv, uint32_t k, I s, uint32_t jlo,
+                                            uint32_t jhi, const L2Policies& pol, float& m, Tracker<I>& t) {
+    float v[8];
+    load_level_sector(lv, k, s, pol, v);
+    take_sector<ARGMIN, RIGHT>(v, k, s, jlo, jhi, m, t);
+}
+
+// Ascending scan of [lo, hi) (lo < hi) at level k, two sectors per round
+// trip.
 template <bool ARGMIN, typename I>
 __device__ __forceinline__ void scan_fwd(const LevelsT<I>& lv, uint32_t k, I lo, I hi,
                                          const L2Policies& pol, float& m, Tracker<I>& t) {
-    for (I s = lo & ~I(7); s < hi; s += 8u) {
+    I s = lo & ~I(7);
+    for (; s + 8u < hi; s += 16u) {
+        // Sector s ends before hi; sector s + 8 starts before hi.
+        float a[8], b[8];
+        load_level_sector(lv, k, s, pol, a);
+        load_level_sector(lv, k, s + 8u, pol, b);
+        const I s2 = s + 8u;
+        take_sector<ARGMIN, false>(a, k, s, s < lo ? uint32_t(lo - s) : 0u, 8u, m, t);
+        take_sector<ARGMIN, false>(b, k, s2, 0u, hi - s2 < 8u ? uint32_t(hi - s2) : 8u, m, t);
+    }
+    if (s < hi) {
         const uint32_t jlo = s < lo ? uint32_t(lo - s) : 0u;
         const uint32_t jhi = hi - s < 8u ? uint32_t(hi - s) : 8u;
         scan_sector<ARGMIN, false>(lv, k, s, jlo, jhi, pol, m, t);
