@@ -194,9 +194,11 @@ def barrier(ws: int):
 
 
 # ---------------------------------------------------------------------------
-def make_inputs(n: int, q: int, lr: int, seed: int):
+def make_inputs(n: int, q: int, lr: int, seed: int, ties: float = 0.0):
     import rmq_gb300 as R
     a = R.gen_array(n, seed)
+    if ties > 0.0:
+        R.plant_min_ties(a, ties, seed)
     qs = R.gen_queries(q, lr, n, seed)
     return a, qs
 
@@ -228,7 +230,7 @@ def run_reference(args, ws, rank):
     if rank != 0:
         return
     from oracle import oracle
-    a, qs = make_inputs(args.n, args.q, args.lr, args.seed)
+    a, qs = make_inputs(args.n, args.q, args.lr, args.seed, args.ties)
     threads = oracle.max_threads()
     per_step = args.ref_step_queries
     rng = np.random.default_rng(args.seed)
@@ -257,11 +259,25 @@ def run_reference(args, ws, rank):
     print(json.dumps(line), flush=True)
 
 
+LENGTH_LAWS = {
+    -1: "len uniform in [1,n]",
+    -2: "len lognormal(median n^0.6, sigma 0.3)",
+    -3: "len lognormal(median n^0.3, sigma 0.3)",
+    -4: "len lognormal(median n/2^8, sigma 0.3)",
+    -5: "len lognormal(median n/2^15, sigma 0.3)",
+    -6: "len mixture of the laws -1/-2/-3",
+    -7: "len=clamp(round(exp(N(ln 2^13,1))),1,n)",
+    -8: "len one third each uniform [1,n], lognormal(2^13, 1.0), lognormal(2^5, 0.7), clamped",
+}
+
+
 def workload_config(args) -> dict:
-    return {"workload": f"plain single array: n=2^{int(np.log2(args.n))} fp32 uniform[0,1), "
-                        f"q=2^{int(np.log2(args.q))} queries, len=clamp(round(exp(N(ln 2^13,1))),1,n), "
+    law = LENGTH_LAWS.get(args.lr, f"len = {args.lr}" if args.lr > 0 else f"length law {args.lr}")
+    ties = f" with {100 * args.ties:g} % of entries set to the global minimum" if args.ties > 0 else ""
+    return {"workload": f"plain single array: n=2^{np.log2(args.n):g} fp32 uniform[0,1){ties}, "
+                        f"q=2^{np.log2(args.q):g} queries, {law}, "
                         f"l uniform in [0,n-len]; min + argmin per query",
-            "n": args.n, "q": args.q, "lr_code": args.lr, "seed": args.seed,
+            "n": args.n, "q": args.q, "lr_code": args.lr, "seed": args.seed, "ties": args.ties,
             "variant": args.variant, "scan_threshold": args.t, "rf_log": args.rf_log, "lanes": args.lanes,
             "l2": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{dist_env()[0]}"}
 
@@ -274,7 +290,7 @@ def run_ours(args, ws, rank, local):
     dev = torch.device("cuda", local)
     dist_init(ws, "nccl")
 
-    a, qs = make_inputs(args.n, args.q, args.lr, args.seed + rank)
+    a, qs = make_inputs(args.n, args.q, args.lr, args.seed + rank, args.ties)
     q = qs.shape[0]
     dv = torch.from_numpy(a).to(dev)
     dq = torch.from_numpy(qs.view(np.int32)).to(dev)
@@ -334,7 +350,7 @@ def run_ours(args, ws, rank, local):
     min_only_qps = q * args.steps / (e0.elapsed_time(e1) / 1e3)
 
     # --- end to end: pinned host queries -> device -> host results -------------
-    e2e = run_e2e(args, h, qs, dev, ws)
+    e2e = run_e2e(args, h, qs, dev, ws, out_idx, out_min)
 
     # --- parity spot check of the timed outputs (not timed) ---------------------
     from oracle import oracle
@@ -419,57 +435,24 @@ def run_ours(args, ws, rank, local):
         dist.destroy_process_group()
 
 
-def run_e2e(args, h, qs, dev, ws) -> dict:
-    """Same metric through the C ABI with host buffers: every step copies the
-    queries from pinned host memory, answers them and copies min + argmin back,
-    in chunks pipelined over two streams (copy of chunk i+1 overlaps the
-    kernel of chunk i and the copy back of chunk i-1)."""
+def run_e2e(args, h, qs, dev, ws, out_idx, out_min) -> dict:
+    """Same metric through the C ABI with host buffers: every step is one
+    rmq_query_idx_host call on page-locked host buffers (queries in, min +
+    argmin out); with page-locked buffers the library's kernel reads the
+    queries from and writes the results to host memory directly.  The results
+    must equal those of the device-buffer call."""
     import torch
     q = qs.shape[0]
-    chunk = min(q, args.e2e_chunk)
-    nchunks = (q + chunk - 1) // chunk
     h_q = torch.from_numpy(qs.view(np.int32).reshape(-1)).pin_memory()
     h_min = torch.empty(q, dtype=torch.float32).pin_memory()
     h_idx = torch.empty(q, dtype=torch.int32).pin_memory()
-    nbuf = 3
-    d_q = [torch.empty(2 * chunk, dtype=torch.int32, device=dev) for _ in range(nbuf)]
-    d_min = [torch.empty(chunk, dtype=torch.float32, device=dev) for _ in range(nbuf)]
-    d_idx = [torch.empty(chunk, dtype=torch.int32, device=dev) for _ in range(nbuf)]
-    s_h2d = torch.cuda.Stream(device=dev)
-    s_cmp = torch.cuda.Stream(device=dev)
-    s_d2h = torch.cuda.Stream(device=dev)
-    launches = [0]
 
     def one_pass():
-        done_h2d = [torch.cuda.Event() for _ in range(nchunks)]
-        done_cmp = [torch.cuda.Event() for _ in range(nchunks)]
-        done_d2h = [None] * nbuf
-        for c in range(nchunks):
-            b = c % nbuf
-            lo = c * chunk
-            m = min(chunk, q - lo)
-            with torch.cuda.stream(s_h2d):
-                if done_d2h[b] is not None:
-                    s_h2d.wait_event(done_d2h[b])
-                d_q[b][: 2 * m].copy_(h_q[2 * lo: 2 * (lo + m)], non_blocking=True)
-                done_h2d[c].record(s_h2d)
-            with torch.cuda.stream(s_cmp):
-                s_cmp.wait_event(done_h2d[c])
-                st = h.query_idx_raw(int(d_q[b].data_ptr()), m, int(d_idx[b].data_ptr()),
-                                     int(d_min[b].data_ptr()), s_cmp.cuda_stream)
-                if st != 0:
-                    raise RuntimeError(f"rmq_query_idx failed: {st}")
-                launches[0] += 1
-                done_cmp[c].record(s_cmp)
-            with torch.cuda.stream(s_d2h):
-                s_d2h.wait_event(done_cmp[c])
-                h_min[lo: lo + m].copy_(d_min[b][:m], non_blocking=True)
-                h_idx[lo: lo + m].copy_(d_idx[b][:m], non_blocking=True)
-                ev = torch.cuda.Event()
-                ev.record(s_d2h)
-                done_d2h[b] = ev
+        st = h.query_idx_host_raw(int(h_q.data_ptr()), q, int(h_idx.data_ptr()), int(h_min.data_ptr()))
+        if st != 0:
+            raise RuntimeError(f"rmq_query_idx_host failed: {st}")
 
-    for _ in range(args.warmup):
+    for _ in range(max(1, args.warmup)):
         one_pass()
     torch.cuda.synchronize()
     barrier(ws)
@@ -478,8 +461,11 @@ def run_e2e(args, h, qs, dev, ws) -> dict:
         one_pass()
     torch.cuda.synchronize()
     dt = max_over_ranks(time.perf_counter() - t0, ws, dev)
+    same = bool(torch.equal(h_idx, out_idx.cpu()) and torch.equal(h_min.view(torch.int32), out_min.cpu().view(torch.int32)))
     return {"value": ws * q * args.steps / dt, "unit": UNIT, "h2d_bytes_per_step": 8 * q,
-            "d2h_bytes_per_step": 8 * q, "chunk_queries": chunk, "kernel_launches_per_step": nchunks}
+            "d2h_bytes_per_step": 8 * q,
+            "api": "rmq_query_idx_host on page-locked host buffers (kernel reads / writes host memory)",
+            "kernel_launches_per_step": 1, "results_equal_device_call": same}
 
 
 def run_batched(args, ws, rank, local):
@@ -764,12 +750,13 @@ def parse_args(argv=None):
     ap.add_argument("--q", type=int, default=1 << 26)
     ap.add_argument("--lr", type=int, default=-7, help="length law code (-7 = lognormal median 2^13 sigma 1)")
     ap.add_argument("--seed", type=int, default=42)
+    ap.add_argument("--ties", type=float, default=0.0,
+                    help="fraction of entries set to the global minimum (the large mixed workload uses 0.01)")
     ap.add_argument("--variant", default="auto", choices=["auto", "cl", "vl"])
     ap.add_argument("--t", type=int, default=1 << 10, help="scan threshold")
     ap.add_argument("--rf-log", dest="rf_log", type=int, default=0)
     ap.add_argument("--lanes", type=int, default=0)
     ap.add_argument("--l2-persist", dest="l2_persist", action="store_true")
-    ap.add_argument("--e2e-chunk", dest="e2e_chunk", type=int, default=1 << 22)
     ap.add_argument("--cpu-budget", dest="cpu_budget", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", dest="no_cpu_baseline", action="store_true")
     ap.add_argument("--no-reference-gpu", dest="no_reference_gpu", action="store_true")

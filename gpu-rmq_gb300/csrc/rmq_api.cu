@@ -35,6 +35,19 @@ struct rmq_handle {
     float persist_hit_ratio = 1.f;
     float build_ms = 0.f;
     std::mutex validate_mu;
+
+    // Staging of the host-buffer calls (rmq_query_host / rmq_query_idx_host),
+    // created on the first such call.
+    struct HostPipe {
+        static constexpr int kBufs = 3;
+        std::mutex mu;
+        uint64_t chunk = 0;  // queries per staging buffer
+        void* d_q[kBufs] = {};
+        float* d_min[kBufs] = {};
+        void* d_idx[kBufs] = {};
+        cudaStream_t up = nullptr, run = nullptr, down = nullptr;
+        cudaEvent_t ev_up[kBufs] = {}, ev_run[kBufs] = {}, ev_down[kBufs] = {};
+    } pipe;
 };
 
 namespace {
@@ -251,20 +264,9 @@ int rmq_build(const float* d_values, uint64_t n, const rmq_config* cfg, rmq_stre
     return RMQ_OK;
 }
 
-static int query_common(const rmq_handle* hc, const void* d_lr, uint64_t q, float* d_min, void* d_argmin,
-                        bool wide_call, rmq_stream_t stream) {
-    if (hc == nullptr) return RMQ_ERR_ARG;
-    if (hc->wide != wide_call) return RMQ_ERR_UNSUPPORTED;
-    if (q == 0) return RMQ_OK;
-    if (!wide_call && q > 0xFFFFFFFFull) return RMQ_ERR_UNSUPPORTED;
-    const uintptr_t qalign = wide_call ? 15u : 7u;
-    if (d_lr == nullptr || (reinterpret_cast<uintptr_t>(d_lr) & qalign) != 0) return RMQ_ERR_ARG;
-    if (d_min == nullptr && d_argmin == nullptr) return RMQ_ERR_ARG;
-    if (d_argmin != nullptr && !hc->with_index && hc->lay.num_levels > 1) return RMQ_ERR_NO_INDEX;
-    rmq_handle* h = const_cast<rmq_handle*>(hc);
-    DeviceGuard guard(h->device);
-    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-
+// Launch arguments of one query call on device buffers (err left null).
+static rmq::QueryArgs query_args(const rmq_handle* h, const void* d_lr, uint64_t q, float* d_min,
+                                 void* d_argmin) {
     rmq::QueryArgs a;
     std::memset(&a, 0, sizeof(a));
     for (uint32_t k = 0; k < h->lay.num_levels; ++k) {
@@ -297,6 +299,23 @@ static int query_common(const rmq_handle* hc, const void* d_lr, uint64_t q, floa
     a.persist_base = h->persist_bytes ? h->val_buf : nullptr;
     a.persist_bytes = h->persist_bytes;
     a.persist_hit_ratio = h->persist_hit_ratio;
+    return a;
+}
+
+static int query_common(const rmq_handle* hc, const void* d_lr, uint64_t q, float* d_min, void* d_argmin,
+                        bool wide_call, rmq_stream_t stream) {
+    if (hc == nullptr) return RMQ_ERR_ARG;
+    if (hc->wide != wide_call) return RMQ_ERR_UNSUPPORTED;
+    if (q == 0) return RMQ_OK;
+    if (!wide_call && q > 0xFFFFFFFFull) return RMQ_ERR_UNSUPPORTED;
+    const uintptr_t qalign = wide_call ? 15u : 7u;
+    if (d_lr == nullptr || (reinterpret_cast<uintptr_t>(d_lr) & qalign) != 0) return RMQ_ERR_ARG;
+    if (d_min == nullptr && d_argmin == nullptr) return RMQ_ERR_ARG;
+    if (d_argmin != nullptr && !hc->with_index && hc->lay.num_levels > 1) return RMQ_ERR_NO_INDEX;
+    rmq_handle* h = const_cast<rmq_handle*>(hc);
+    DeviceGuard guard(h->device);
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    rmq::QueryArgs a = query_args(h, d_lr, q, d_min, d_argmin);
 
     if (!h->validate) {
         a.err = nullptr;
@@ -311,6 +330,203 @@ static int query_common(const rmq_handle* hc, const void* d_lr, uint64_t q, floa
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return cuda_status(e);
     return bad ? RMQ_ERR_QUERY_RANGE : RMQ_OK;
+}
+
+
+// Queries per staging buffer of the host-buffer calls: large enough that the
+// per-chunk launch and copy overheads are small against a chunk's kernel
+// time, small enough that the first upload and the last download (which
+// nothing overlaps) stay short.
+#ifndef RMQ_HOST_CHUNK_LOG
+#define RMQ_HOST_CHUNK_LOG 22  // tuning knob
+#endif
+constexpr uint64_t kHostChunk = uint64_t(1) << RMQ_HOST_CHUNK_LOG;
+
+static void free_pipe(rmq_handle::HostPipe& p) {
+    for (int b = 0; b < rmq_handle::HostPipe::kBufs; ++b) {
+        if (p.d_q[b]) cudaFree(p.d_q[b]);
+        if (p.d_min[b]) cudaFree(p.d_min[b]);
+        if (p.d_idx[b]) cudaFree(p.d_idx[b]);
+        if (p.ev_up[b]) cudaEventDestroy(p.ev_up[b]);
+        if (p.ev_run[b]) cudaEventDestroy(p.ev_run[b]);
+        if (p.ev_down[b]) cudaEventDestroy(p.ev_down[b]);
+        p.d_q[b] = nullptr;
+        p.d_min[b] = nullptr;
+        p.d_idx[b] = nullptr;
+        p.ev_up[b] = p.ev_run[b] = p.ev_down[b] = nullptr;
+    }
+    if (p.up) cudaStreamDestroy(p.up);
+    if (p.run) cudaStreamDestroy(p.run);
+    if (p.down) cudaStreamDestroy(p.down);
+    p.up = p.run = p.down = nullptr;
+    p.chunk = 0;
+    cudaGetLastError();
+}
+
+// Staging for chunks of `chunk` queries (caller holds p.mu).
+// (chunk = 0: streams and events only.)
+static cudaError_t ensure_pipe(rmq_handle* h, uint64_t chunk) {
+    rmq_handle::HostPipe& p = h->pipe;
+    if (p.run != nullptr && p.chunk >= chunk) return cudaSuccess;
+    free_pipe(p);
+    const size_t qbytes = chunk * (h->wide ? 2 * sizeof(uint64_t) : 2 * sizeof(uint32_t));
+    const size_t ibytes = chunk * (h->wide ? sizeof(uint64_t) : sizeof(uint32_t));
+    cudaError_t e = cudaSuccess;
+    for (int b = 0; b < rmq_handle::HostPipe::kBufs && e == cudaSuccess; ++b) {
+        if (chunk > 0) {
+            e = cudaMalloc(&p.d_q[b], qbytes);
+            if (e == cudaSuccess) e = cudaMalloc(&p.d_min[b], chunk * sizeof(float));
+            if (e == cudaSuccess) e = cudaMalloc(&p.d_idx[b], ibytes);
+        }
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p.ev_up[b], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p.ev_run[b], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p.ev_down[b], cudaEventDisableTiming);
+    }
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p.up, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p.run, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p.down, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        free_pipe(p);
+        return e;
+    }
+    p.chunk = chunk;
+    return cudaSuccess;
+}
+
+// Device address of host memory the device can read and write directly
+// (page-locked: cudaHostAlloc / cudaHostRegister), aligned to `align` bytes;
+// nullptr otherwise.
+static void* mapped_host(const void* p, uintptr_t align) {
+    if (p == nullptr || (reinterpret_cast<uintptr_t>(p) & (align - 1)) != 0) return nullptr;
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (at.type != cudaMemoryTypeHost || at.devicePointer == nullptr) return nullptr;
+    return at.devicePointer;
+}
+
+// Host-buffer queries.  When every host buffer is page-locked, one kernel
+// launch reads the queries and writes the results in host memory directly
+// (no staging, no copy-engine passes).  Otherwise chunks of the host query
+// array are uploaded into one of three device staging buffers, answered and
+// downloaded, the upload of chunk c + 1 and the download of chunk c - 1
+// overlapping the kernel of chunk c (three streams; a buffer is reused once
+// its download is done).
+static int query_host_common(const rmq_handle* hc, const void* h_lr, uint64_t q, float* h_min, void* h_argmin,
+                             bool wide_call) {
+    if (hc == nullptr) return RMQ_ERR_ARG;
+    if (hc->wide != wide_call) return RMQ_ERR_UNSUPPORTED;
+    if (q == 0) return RMQ_OK;
+    if (!wide_call && q > 0xFFFFFFFFull) return RMQ_ERR_UNSUPPORTED;
+    if (h_lr == nullptr || (h_min == nullptr && h_argmin == nullptr)) return RMQ_ERR_ARG;
+    if (h_argmin != nullptr && !hc->with_index && hc->lay.num_levels > 1) return RMQ_ERR_NO_INDEX;
+    rmq_handle* h = const_cast<rmq_handle*>(hc);
+    DeviceGuard guard(h->device);
+    rmq_handle::HostPipe& p = h->pipe;
+    std::lock_guard<std::mutex> lock(p.mu);
+    const size_t qsize = wide_call ? 2 * sizeof(uint64_t) : 2 * sizeof(uint32_t);
+    const size_t isize = wide_call ? sizeof(uint64_t) : sizeof(uint32_t);
+
+    void* m_lr = mapped_host(h_lr, qsize);
+    void* m_min = h_min != nullptr ? mapped_host(h_min, sizeof(float)) : nullptr;
+    void* m_idx = h_argmin != nullptr ? mapped_host(h_argmin, isize) : nullptr;
+    if (m_lr != nullptr && (h_min == nullptr || m_min != nullptr) && (h_argmin == nullptr || m_idx != nullptr)) {
+        cudaError_t e = ensure_pipe(h, 0);
+        if (e != cudaSuccess) return cuda_status(e);
+        std::unique_lock<std::mutex> vlock;
+        rmq::QueryArgs a = query_args(h, m_lr, q, static_cast<float*>(m_min), m_idx);
+        uint32_t bad = 0;
+        if (h->validate) {
+            vlock = std::unique_lock<std::mutex>(h->validate_mu);
+            a.err = h->err;
+            e = cudaMemsetAsync(h->err, 0, sizeof(uint32_t), p.run);
+        }
+        if (e == cudaSuccess) e = rmq::launch_query(a, p.run);
+        if (e == cudaSuccess && h->validate)
+            e = cudaMemcpyAsync(&bad, h->err, sizeof(uint32_t), cudaMemcpyDeviceToHost, p.run);
+        const cudaError_t es = cudaStreamSynchronize(p.run);
+        if (e == cudaSuccess) e = es;
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return cuda_status(e);
+        }
+        return bad ? RMQ_ERR_QUERY_RANGE : RMQ_OK;
+    }
+
+    cudaError_t e = ensure_pipe(h, q < kHostChunk ? q : kHostChunk);
+    if (e != cudaSuccess) return cuda_status(e);
+    const uint64_t chunk = q < p.chunk ? q : p.chunk;
+    const char* src = static_cast<const char*>(h_lr);
+    char* dst_idx = static_cast<char*>(h_argmin);
+
+    // The error counter is shared with the device-buffer calls in validate mode.
+    std::unique_lock<std::mutex> vlock;
+    if (h->validate) {
+        vlock = std::unique_lock<std::mutex>(h->validate_mu);
+        e = cudaMemsetAsync(h->err, 0, sizeof(uint32_t), p.run);
+    }
+    const uint64_t nchunks = (q + chunk - 1) / chunk;
+    for (uint64_t c = 0; c < nchunks && e == cudaSuccess; ++c) {
+        const int b = int(c % rmq_handle::HostPipe::kBufs);
+        const uint64_t lo = c * chunk;
+        const uint64_t m = q - lo < chunk ? q - lo : chunk;
+        if (c >= uint64_t(rmq_handle::HostPipe::kBufs)) e = cudaStreamWaitEvent(p.up, p.ev_down[b], 0);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(p.d_q[b], src + lo * qsize, m * qsize, cudaMemcpyHostToDevice, p.up);
+        if (e == cudaSuccess) e = cudaEventRecord(p.ev_up[b], p.up);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(p.run, p.ev_up[b], 0);
+        if (e == cudaSuccess) {
+            rmq::QueryArgs a = query_args(h, p.d_q[b], m, h_min ? p.d_min[b] : nullptr,
+                                          h_argmin ? p.d_idx[b] : nullptr);
+            a.err = h->validate ? h->err : nullptr;
+            e = rmq::launch_query(a, p.run);
+        }
+        if (e == cudaSuccess) e = cudaEventRecord(p.ev_run[b], p.run);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(p.down, p.ev_run[b], 0);
+        if (e == cudaSuccess && h_argmin)
+            e = cudaMemcpyAsync(dst_idx + lo * isize, p.d_idx[b], m * isize, cudaMemcpyDeviceToHost, p.down);
+        if (e == cudaSuccess && h_min)
+            e = cudaMemcpyAsync(h_min + lo, p.d_min[b], m * sizeof(float), cudaMemcpyDeviceToHost, p.down);
+        if (e == cudaSuccess) e = cudaEventRecord(p.ev_down[b], p.down);
+    }
+    uint32_t bad = 0;
+    if (e == cudaSuccess && h->validate) {
+        e = cudaStreamWaitEvent(p.down, p.ev_run[int((nchunks - 1) % rmq_handle::HostPipe::kBufs)], 0);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&bad, h->err, sizeof(uint32_t), cudaMemcpyDeviceToHost, p.down);
+    }
+    // Drain all three streams even after a failure: staging buffers must be idle.
+    const cudaError_t e1 = cudaStreamSynchronize(p.up);
+    const cudaError_t e2 = cudaStreamSynchronize(p.run);
+    const cudaError_t e3 = cudaStreamSynchronize(p.down);
+    if (e == cudaSuccess) e = e1 != cudaSuccess ? e1 : (e2 != cudaSuccess ? e2 : e3);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return cuda_status(e);
+    }
+    return bad ? RMQ_ERR_QUERY_RANGE : RMQ_OK;
+}
+
+int rmq_query_host(const rmq_handle* h, const uint32_t* h_lr, uint64_t q, float* h_min) {
+    if (h_min == nullptr) return RMQ_ERR_ARG;
+    return query_host_common(h, h_lr, q, h_min, nullptr, false);
+}
+
+int rmq_query_idx_host(const rmq_handle* h, const uint32_t* h_lr, uint64_t q, uint32_t* h_argmin,
+                       float* h_min_or_null) {
+    if (h_argmin == nullptr) return RMQ_ERR_ARG;
+    return query_host_common(h, h_lr, q, h_min_or_null, h_argmin, false);
+}
+
+int rmq_query64_host(const rmq_handle* h, const uint64_t* h_lr, uint64_t q, float* h_min) {
+    if (h_min == nullptr) return RMQ_ERR_ARG;
+    return query_host_common(h, h_lr, q, h_min, nullptr, true);
+}
+
+int rmq_query_idx64_host(const rmq_handle* h, const uint64_t* h_lr, uint64_t q, uint64_t* h_argmin,
+                         float* h_min_or_null) {
+    if (h_argmin == nullptr) return RMQ_ERR_ARG;
+    return query_host_common(h, h_lr, q, h_min_or_null, h_argmin, true);
 }
 
 int rmq_query(const rmq_handle* h, const uint32_t* d_lr, uint64_t q, float* d_min,
@@ -365,6 +581,7 @@ void rmq_destroy(rmq_handle* h) {
     if (h == nullptr) return;
     {
         DeviceGuard guard(h->device);
+        free_pipe(h->pipe);
         if (h->val_buf) cudaFree(h->val_buf);
         if (h->err) cudaFree(h->err);
         cudaGetLastError();

@@ -111,6 +111,14 @@ def lib() -> ctypes.CDLL:
         L.rmq_query64.restype = ctypes.c_int
         L.rmq_query_idx64.argtypes = [_P, _P, _U64, _P, _P, _P]
         L.rmq_query_idx64.restype = ctypes.c_int
+        L.rmq_query_host.argtypes = [_P, _P, _U64, _P]
+        L.rmq_query_host.restype = ctypes.c_int
+        L.rmq_query_idx_host.argtypes = [_P, _P, _U64, _P, _P]
+        L.rmq_query_idx_host.restype = ctypes.c_int
+        L.rmq_query64_host.argtypes = [_P, _P, _U64, _P]
+        L.rmq_query64_host.restype = ctypes.c_int
+        L.rmq_query_idx64_host.argtypes = [_P, _P, _U64, _P, _P]
+        L.rmq_query_idx64_host.restype = ctypes.c_int
         L.rmq_scan_bruteforce.argtypes = [_P, _U64, _P, _U64, _P, _P, _P]
         L.rmq_scan_bruteforce.restype = ctypes.c_int
         L.rmq_get_info.argtypes = [_P, ctypes.POINTER(RMQInfo)]
@@ -271,6 +279,36 @@ class Hierarchy:
                                    _dev_ptr(out_min) if out_min is not None else None, _stream_handle(stream))
         if st != RMQ_OK:
             raise RMQError(st, "rmq_query_idx64")
+        return (out_idx, out_min) if with_min else out_idx
+
+    def query_idx_host_raw(self, lr_ptr: int, q: int, out_idx_ptr: int, out_min_ptr: int | None) -> int:
+        """rmq_query_idx_host on host pointers (blocking)."""
+        return lib().rmq_query_idx_host(self._h, lr_ptr, q, out_idx_ptr, out_min_ptr or None)
+
+    def query_host(self, lr: np.ndarray) -> np.ndarray:
+        """Minima of host queries (numpy [q, 2] uint32 or uint64) into a host array."""
+        lr = np.ascontiguousarray(lr)
+        q = lr.shape[0]
+        out = np.empty(q, dtype=np.float32)
+        wide = lr.dtype.itemsize == 8
+        fn = lib().rmq_query64_host if wide else lib().rmq_query_host
+        st = fn(self._h, lr.ctypes.data, q, out.ctypes.data)
+        if st != RMQ_OK:
+            raise RMQError(st, "rmq_query64_host" if wide else "rmq_query_host")
+        return out
+
+    def query_idx_host(self, lr: np.ndarray, with_min: bool = False):
+        """Argmin (and optionally minima) of host queries into host arrays."""
+        lr = np.ascontiguousarray(lr)
+        q = lr.shape[0]
+        wide = lr.dtype.itemsize == 8
+        out_idx = np.empty(q, dtype=np.uint64 if wide else np.uint32)
+        out_min = np.empty(q, dtype=np.float32) if with_min else None
+        fn = lib().rmq_query_idx64_host if wide else lib().rmq_query_idx_host
+        st = fn(self._h, lr.ctypes.data, q, out_idx.ctypes.data,
+                out_min.ctypes.data if out_min is not None else None)
+        if st != RMQ_OK:
+            raise RMQError(st, "rmq_query_idx64_host" if wide else "rmq_query_idx_host")
         return (out_idx, out_min) if with_min else out_idx
 
     def close(self) -> None:

@@ -114,6 +114,25 @@ int rmq_query64(const rmq_handle* h, const uint64_t* d_lr, uint64_t q, float* d_
 int rmq_query_idx64(const rmq_handle* h, const uint64_t* d_lr, uint64_t q, uint64_t* d_argmin,
                     float* d_min_or_null, rmq_stream_t stream);
 
+/* The same queries with HOST buffers, the form of the reference's host
+ * drivers (xxx_rmq / hierarchical_vector_load return a host array,
+ * src/xxx.h:203-298, :932-1040).  h_lr holds the q inclusive pairs in host
+ * memory; results are written to host memory.  Blocking: returns when every
+ * result is in place; calls on one handle are serialised (on streams the
+ * handle owns, created on the first call and kept until rmq_destroy).
+ * When every buffer is page-locked (cudaHostAlloc / cudaHostRegister) and
+ * naturally aligned, one kernel launch reads the queries from and writes the
+ * results to host memory directly.  Otherwise chunks of 2^22 queries go
+ * through device staging buffers (three chunks, allocated on first use and
+ * kept), the upload of one chunk and the download of the previous one
+ * overlapping the kernel of the current one. */
+int rmq_query_host(const rmq_handle* h, const uint32_t* h_lr, uint64_t q, float* h_min);
+int rmq_query_idx_host(const rmq_handle* h, const uint32_t* h_lr, uint64_t q, uint32_t* h_argmin,
+                       float* h_min_or_null);
+int rmq_query64_host(const rmq_handle* h, const uint64_t* h_lr, uint64_t q, float* h_min);
+int rmq_query_idx64_host(const rmq_handle* h, const uint64_t* h_lr, uint64_t q, uint64_t* h_argmin,
+                         float* h_min_or_null);
+
 /* Brute-force scan, one thread per query (the reference's GPU checker,
  * kernel_rmq_basic / kernel_rmq_basic_idx, src/cuda_methods.cuh:4-44).
  * Either output may be NULL.  Used by the driver's --check and as alg 2/102. */

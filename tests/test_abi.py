@@ -95,6 +95,10 @@ def test_bad_arguments_rejected_before_device_work():
     assert L.rmq_build(0x1000, 10, ctypes.byref(bad), None, ctypes.byref(h)) == R.RMQ_ERR_ARG
     assert L.rmq_query(None, 0x1000, 10, 0x2000, None) == R.RMQ_ERR_ARG
     assert L.rmq_query_idx(None, 0x1000, 10, 0x2000, None, None) == R.RMQ_ERR_ARG
+    assert L.rmq_query_host(None, 0x1000, 10, 0x2000) == R.RMQ_ERR_ARG
+    assert L.rmq_query_idx_host(None, 0x1000, 10, 0x2000, None) == R.RMQ_ERR_ARG
+    assert L.rmq_query64_host(None, 0x1000, 10, 0x2000) == R.RMQ_ERR_ARG
+    assert L.rmq_query_idx64_host(None, 0x1000, 10, 0x2000, None) == R.RMQ_ERR_ARG
     assert L.rmq_scan_bruteforce(None, 10, 0x1000, 1, 0x2000, None, None) == R.RMQ_ERR_ARG
     assert L.rmq_scan_bruteforce(0x1000, 10, 0x1004, 1, 0x2000, None, None) == R.RMQ_ERR_ARG
     assert L.rmq_get_info(None, None) == R.RMQ_ERR_ARG
