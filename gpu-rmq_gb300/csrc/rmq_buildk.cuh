@@ -56,26 +56,54 @@ __device__ __forceinline__ void fused_tile(const float* __restrict__ a, P n, con
     const uint64_t base = uint64_t(tile) * kTile;
     const uint64_t pol = policy_evict_first();
 
-    // Stage 0: per-sector first minimum.
+    // Stage 0: per-sector first minimum.  A whole tile inside the array (all
+    // but the last) loads its four sectors per thread at once, takes each
+    // sector's minimum with three 3-input min.f32 and then the first entry
+    // equal to it (its own bits, so a zero keeps the sign of its first
+    // occurrence); the last tile goes entry by entry.
+    constexpr uint32_t kSecPer = kTileSectors / kFusedThreads;
+    if (base + kTile <= uint64_t(n)) {
+        float v[kSecPer][8];
 #pragma unroll
-    for (uint32_t i = 0; i < kTileSectors / kFusedThreads; ++i) {
-        const uint32_t sec = tid + kFusedThreads * i;
-        const uint64_t s = base + 8u * sec;
-        VP c{f_inf(), kNone};
-        if (s < n) {
-            float v[8];
-            if (s + 8u <= n) {
-                ld_sector_policy(a + s, v, pol);
-            } else {
+        for (uint32_t i = 0; i < kSecPer; ++i) ld_sector_policy(a + base + 8u * (tid + kFusedThreads * i), v[i], pol);
 #pragma unroll
-                for (int j = 0; j < 8; ++j) v[j] = (s + j < n) ? a[s + j] : f_inf();
+        for (uint32_t i = 0; i < kSecPer; ++i) {
+            const uint32_t sec = tid + kFusedThreads * i;
+            const float m = fmin3(fmin3(v[i][0], v[i][1], v[i][2]), fmin3(v[i][3], v[i][4], v[i][5]),
+                                  fminf(v[i][6], v[i][7]));
+            uint32_t j = 7;
+            float mv = v[i][7];
+#pragma unroll
+            for (int jj = 6; jj >= 0; --jj) {
+                if (v[i][jj] == m) {
+                    j = uint32_t(jj);
+                    mv = v[i][jj];
+                }
             }
-#pragma unroll
-            for (int j = 0; j < 8; ++j)
-                if (s + j < n) vp_take(c, v[j], P(s + j));
+            sv[sec] = mv;
+            sp[sec] = P(base + 8u * sec + j);
         }
-        sv[sec] = c.v;
-        sp[sec] = c.p;
+    } else {
+#pragma unroll
+        for (uint32_t i = 0; i < kSecPer; ++i) {
+            const uint32_t sec = tid + kFusedThreads * i;
+            const uint64_t s = base + 8u * sec;
+            VP c{f_inf(), kNone};
+            if (s < n) {
+                float v[8];
+                if (s + 8u <= n) {
+                    ld_sector_policy(a + s, v, pol);
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) v[j] = (s + j < n) ? a[s + j] : f_inf();
+                }
+#pragma unroll
+                for (int j = 0; j < 8; ++j)
+                    if (s + j < n) vp_take(c, v[j], P(s + j));
+            }
+            sv[sec] = c.v;
+            sp[sec] = c.p;
+        }
     }
     __syncthreads();
 
