@@ -176,6 +176,7 @@ int rmq_plan_layout(uint64_t n, uint64_t scan_threshold, int32_t rf_log, int32_t
 
 int rmq_build(const float* d_values, uint64_t n, const rmq_config* cfg, rmq_stream_t stream,
               rmq_handle** out) {
+    rmq::NvtxRange nvtx_range("rmq_build");
     if (out == nullptr) return RMQ_ERR_ARG;
     *out = nullptr;
     if (d_values == nullptr || n == 0) return RMQ_ERR_ARG;
@@ -304,6 +305,7 @@ static rmq::QueryArgs query_args(const rmq_handle* h, const void* d_lr, uint64_t
 
 static int query_common(const rmq_handle* hc, const void* d_lr, uint64_t q, float* d_min, void* d_argmin,
                         bool wide_call, rmq_stream_t stream) {
+    rmq::NvtxRange nvtx_range("rmq_query");
     if (hc == nullptr) return RMQ_ERR_ARG;
     if (hc->wide != wide_call) return RMQ_ERR_UNSUPPORTED;
     if (q == 0) return RMQ_OK;
@@ -416,6 +418,7 @@ static void* mapped_host(const void* p, uintptr_t align) {
 // its download is done).
 static int query_host_common(const rmq_handle* hc, const void* h_lr, uint64_t q, float* h_min, void* h_argmin,
                              bool wide_call) {
+    rmq::NvtxRange nvtx_range("rmq_query_host");
     if (hc == nullptr) return RMQ_ERR_ARG;
     if (hc->wide != wide_call) return RMQ_ERR_UNSUPPORTED;
     if (q == 0) return RMQ_OK;

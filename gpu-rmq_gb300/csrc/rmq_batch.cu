@@ -417,6 +417,7 @@ int rmq_batch_set_queries(rmq_batch* b, const uint32_t* d_lr, const uint64_t* qu
 }
 
 int rmq_batch_build(rmq_batch* b, rmq_stream_t stream) {
+    rmq::NvtxRange nvtx_range("rmq_batch_build");
     if (b == nullptr) return RMQ_ERR_ARG;
     DeviceGuard guard(b->device);
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
@@ -428,12 +429,14 @@ int rmq_batch_build(rmq_batch* b, rmq_stream_t stream) {
 }
 
 int rmq_batch_query(rmq_batch* b, rmq_stream_t stream) {
+    rmq::NvtxRange nvtx_range("rmq_batch_query");
     if (b == nullptr || !b->queries_set) return RMQ_ERR_ARG;
     DeviceGuard guard(b->device);
     return status_of(enqueue_query(b, reinterpret_cast<cudaStream_t>(stream)));
 }
 
 int rmq_batch_run(rmq_batch* b, rmq_stream_t stream) {
+    rmq::NvtxRange nvtx_range("rmq_batch_run");
     if (b == nullptr || !b->queries_set) return RMQ_ERR_ARG;
     DeviceGuard guard(b->device);
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
@@ -459,6 +462,7 @@ int rmq_batch_run(rmq_batch* b, rmq_stream_t stream) {
 }
 
 int rmq_batch_autotune(rmq_batch* b, rmq_stream_t stream, rmq_batch_info* info) {
+    rmq::NvtxRange nvtx_range("rmq_batch_autotune");
     if (b == nullptr || !b->queries_set) return RMQ_ERR_ARG;
     DeviceGuard guard(b->device);
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);

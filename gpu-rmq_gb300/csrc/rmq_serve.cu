@@ -261,6 +261,7 @@ void finish_slot(rmq_server* s, Slot& sl) {
 // Packs ready pending requests into a free slot and launches the batch.
 // Called with `lk` held; releases it while packing and launching.
 bool launch_batch(rmq_server* s, Slot& sl, std::unique_lock<std::mutex>& lk) {
+    rmq::NvtxRange nvtx_range("rmq_server_batch");
     const uint64_t max_q = s->cfg.max_batch_queries;
     const uint32_t max_r = s->cfg.max_batch_requests;
     uint64_t nq = 0;
