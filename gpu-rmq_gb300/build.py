@@ -4,6 +4,8 @@ Everything is compiled in-tree with nvcc / g++ / gcc (no cmake), translation
 units in parallel, one -gencode (sm_103a).  Outputs:
 
   gpu-rmq_gb300/librmq_gb300.so      CUDA kernels + C ABI (include/rmq_gb300.h)
+  gpu-rmq_gb300/librmq_gb300_checked.so  the same with bounds-checked level loads
+                                     (RMQ_DEBUG_BOUNDS=1; tests only)
   gpu-rmq_gb300/librmq_gen.so        host input generators (include/rmq_gb300_gen.h)
   gpu-rmq_gb300/driver/rtxrmq        the benchmark driver (reference CLI)
   oracle/liboracle.so                CPU oracle (test infrastructure)
@@ -34,6 +36,7 @@ CUDA_SOURCES = ["rmq_build.cu", "rmq_query.cu", "rmq_api.cu", "rmq_noalloc.cu", 
                 "rmq_gen_device.cu", "rmq_serve.cu"]
 
 LIB = PKG / "librmq_gb300.so"
+CHECKED_LIB = PKG / "librmq_gb300_checked.so"  # bounds-checked build (tests only)
 GENLIB = PKG / "librmq_gen.so"
 DRIVER_BIN = DRIVER / "rtxrmq"
 ORACLE_LIB = ORACLE / "liboracle.so"
@@ -82,22 +85,29 @@ def _headers() -> list[Path]:
 
 
 def build_library(force: bool = False) -> Path:
-    BUILD.mkdir(parents=True, exist_ok=True)
+    """The library and, from the same sources with RMQ_DEBUG_BOUNDS=1, its
+    bounds-checked twin (all translation units compiled in parallel)."""
     nvcc = _nvcc()
     hdrs = _headers()
     jobs = []
-    objs = []
-    for src in CUDA_SOURCES:
-        s = CSRC / src
-        o = BUILD / (s.stem + ".o")
-        objs.append(o)
-        if force or _stale(o, [s] + hdrs):
-            jobs.append([nvcc, *ARCH, *NVCC_FLAGS, "-c", str(s), "-o", str(o)])
+    variants = [(LIB, BUILD, []), (CHECKED_LIB, BUILD / "checked", ["-DRMQ_DEBUG_BOUNDS=1"])]
+    links = []
+    for lib, outdir, flags in variants:
+        outdir.mkdir(parents=True, exist_ok=True)
+        objs = []
+        for src in CUDA_SOURCES:
+            s = CSRC / src
+            o = outdir / (s.stem + ".o")
+            objs.append(o)
+            if force or _stale(o, [s] + hdrs):
+                jobs.append([nvcc, *ARCH, *NVCC_FLAGS, *flags, "-c", str(s), "-o", str(o)])
+        links.append((lib, objs))
     with ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         for f in [ex.submit(_run, j) for j in jobs]:
             f.result()
-    if force or jobs or _stale(LIB, objs):
-        _run([nvcc, *ARCH, "-shared", "-o", str(LIB), *map(str, objs)])
+    for lib, objs in links:
+        if force or _stale(lib, objs):
+            _run([nvcc, *ARCH, "-shared", "-o", str(lib), *map(str, objs)])
     return LIB
 
 

@@ -141,6 +141,19 @@ void rmq_config_init(rmq_config* cfg) {
     cfg->with_index = 1;
 }
 
+int rmq_debug_bounds_violations(uint64_t* count) {
+    if (count == nullptr) return RMQ_ERR_ARG;
+    *count = 0;
+#if RMQ_DEBUG_BOUNDS
+    const unsigned int a = rmq::bounds_bad_query(), b = rmq::bounds_bad_batch();
+    if (a == ~0u || b == ~0u) return RMQ_ERR_CUDA;
+    *count = uint64_t(a) + b;
+    return RMQ_OK;
+#else
+    return RMQ_ERR_UNSUPPORTED;
+#endif
+}
+
 const char* rmq_strerror(int status) {
     switch (status) {
         case RMQ_OK: return "ok";

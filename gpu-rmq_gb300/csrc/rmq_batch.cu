@@ -146,6 +146,10 @@ cudaError_t launch_fill_owner(const uint64_t* unit_off, uint32_t num, uint32_t* 
     return cudaGetLastError();
 }
 
+#if RMQ_DEBUG_BOUNDS
+RMQ_BOUNDS_COUNTER_READER(bounds_bad_batch)
+#endif
+
 cudaError_t launch_batch_query(const BatchQueryArgs& a, cudaStream_t s) {
     if (a.total_units == 0) return cudaSuccess;
     const uint32_t warps = a.threads / 32u;

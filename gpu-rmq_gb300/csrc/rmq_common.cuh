@@ -13,6 +13,35 @@
 
 namespace rmq {
 
+// Bounds-checked builds (-DRMQ_DEBUG_BOUNDS=1: librmq_gb300_checked.so)
+// check every level load of the query kernels before it is made; a load
+// outside its level is counted and skipped (it reads +inf), so the checked
+// build never touches memory out of bounds either.  compute-sanitizer is not
+// available where this library is tested; this is the substitute.
+#ifndef RMQ_DEBUG_BOUNDS
+#define RMQ_DEBUG_BOUNDS 0
+#endif
+#if RMQ_DEBUG_BOUNDS
+// One counter per translation unit (no relocatable device code); each unit
+// that launches checked kernels reads its own through
+// RMQ_BOUNDS_COUNTER_READER.
+static __device__ unsigned int g_rmq_bounds_bad = 0;
+__device__ __forceinline__ bool bounds_ok(bool ok) {
+    if (!ok) atomicAdd(&g_rmq_bounds_bad, 1u);
+    return ok;
+}
+#define RMQ_BOUNDS_COUNTER_READER(name)                                                 \
+    unsigned int name() {                                                               \
+        unsigned int v = 0, z = 0;                                                      \
+        if (cudaMemcpyFromSymbol(&v, g_rmq_bounds_bad, sizeof(v)) != cudaSuccess) {     \
+            cudaGetLastError();                                                         \
+            return ~0u;                                                                 \
+        }                                                                               \
+        cudaMemcpyToSymbol(g_rmq_bounds_bad, &z, sizeof(z));                            \
+        return v;                                                                       \
+    }
+#endif
+
 constexpr int kMaxLevels = 20;            // XXX_MAX_LEVELS, src/constants.cuh:14
 constexpr uint32_t kLevelAlign = 32;      // XXX_LEVEL_ALIGNMENT, src/constants.cuh:15 (entries)
 constexpr uint32_t kNoPos = 0xFFFFFFFFu;  // "no candidate" / invalid-query argmin

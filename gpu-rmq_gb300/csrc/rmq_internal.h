@@ -76,6 +76,13 @@ struct BatchQueryArgs {
 cudaError_t launch_batch_query(const BatchQueryArgs& a, cudaStream_t s);
 cudaError_t launch_fill_owner(const uint64_t* unit_off, uint32_t num, uint32_t* owner, cudaStream_t s);
 
+#if RMQ_DEBUG_BOUNDS
+// Violations counted by the checked kernels of the query / batched units
+// since the last read (each read clears them).
+unsigned int bounds_bad_query();
+unsigned int bounds_bad_batch();
+#endif
+
 // Number of kernel launches the last launch_build issued (for accounting).
 int build_launch_count(const Layout& lay);
 

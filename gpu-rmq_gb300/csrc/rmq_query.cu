@@ -178,7 +178,13 @@ query_cl_kernel(Levels lv, const uint2* __restrict__ qs, uint32_t q, float* __re
 #pragma unroll
                 for (int t = 1; t < 8; ++t) val = (uint32_t(t) == jj) ? v[t] : val;
                 const uint32_t e = b.s + jj;
-                if (out_idx != nullptr) st_stream(out_idx + base + j, k == 0 ? e : ld_index(lv.idx[k] + e));
+#if RMQ_DEBUG_BOUNDS
+                const bool idx_ok = out_idx == nullptr || k == 0 || bounds_ok(lv.idx[k] != nullptr && e < lv.size[k]);
+#else
+                constexpr bool idx_ok = true;
+#endif
+                if (out_idx != nullptr && idx_ok)
+                    st_stream(out_idx + base + j, k == 0 ? e : ld_index(lv.idx[k] + e));
                 if (out_min != nullptr) st_stream(out_min + base + j, val);
             }
         }
@@ -299,6 +305,10 @@ static cudaError_t launch_query_r(const QueryArgs& a, cudaStream_t s) {
     }
 #undef RMQ_CL
 }
+
+#if RMQ_DEBUG_BOUNDS
+RMQ_BOUNDS_COUNTER_READER(bounds_bad_query)
+#endif
 
 cudaError_t launch_query(const QueryArgs& a, cudaStream_t s) {
     if (a.q == 0) return cudaSuccess;

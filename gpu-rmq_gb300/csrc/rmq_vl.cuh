@@ -78,6 +78,15 @@ __device__ __forceinline__ uint64_t ld_index(const uint64_t* p) {
 template <typename I>
 __device__ __forceinline__ void load_level_sector(const LevelsT<I>& lv, uint32_t k, I s,
                                                   const L2Policies& pol, float (&v)[8]) {
+#if RMQ_DEBUG_BOUNDS
+    // Level 0 is read up to its last entry; a coarse level up to its 32-entry padding.
+    if (!bounds_ok(k < lv.num_levels && (s & I(7)) == 0 &&
+                   (k == 0 ? s < lv.size[0] : s + 8u <= ((lv.size[k] + 31u) & ~I(31))))) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) v[j] = f_inf();
+        return;
+    }
+#endif
     const float* base = lv.val[k];
     if (k > 0) {
         ld_sector_policy(base + s, v, pol.coarse);
@@ -319,6 +328,12 @@ __device__ __forceinline__ void vl_locate(const LevelsT<I>& lv, I l, const Track
     load_level_sector(lv, k, w.s, pol, v);
     uint32_t ix[8];
     if constexpr (sizeof(I) == 4) {
+#if RMQ_DEBUG_BOUNDS
+        if (k > 0 && !bounds_ok(lv.idx[k] != nullptr && w.s + 8u <= ((lv.size[k] + 31u) & ~I(31)))) {
+#pragma unroll
+            for (int j = 0; j < 8; ++j) ix[j] = 0u;
+        } else
+#endif
         if (k > 0) ld_sector_u32_policy(lv.idx[k] + w.s, ix, pol.coarse);
     }
     uint32_t j = jlo;
@@ -337,6 +352,12 @@ __device__ __forceinline__ void vl_locate(const LevelsT<I>& lv, I l, const Track
         for (int jj = 1; jj < 8; ++jj) x = (uint32_t(jj) == j) ? ix[jj] : x;
         out_i = k == 0 ? e : x;
     } else {
+#if RMQ_DEBUG_BOUNDS
+        if (k > 0 && !bounds_ok(lv.idx[k] != nullptr && e < lv.size[k])) {
+            out_i = 0;
+            return;
+        }
+#endif
         out_i = k == 0 ? e : ld_index(lv.idx[k] + e);
     }
 }

@@ -127,6 +127,8 @@ def lib() -> ctypes.CDLL:
         L.rmq_destroy.restype = None
         L.rmq_strerror.argtypes = [ctypes.c_int]
         L.rmq_strerror.restype = ctypes.c_char_p
+        L.rmq_debug_bounds_violations.argtypes = [ctypes.POINTER(_U64)]
+        L.rmq_debug_bounds_violations.restype = ctypes.c_int
         L.rmq_plan_layout.argtypes = [_U64, _U64, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(RMQInfo)]
         L.rmq_plan_layout.restype = ctypes.c_int
         _lib = L

@@ -173,6 +173,13 @@ int rmq_query_idx_static(const float* d_values, uint64_t n, uint64_t scan_thresh
                          const uint32_t* d_lr, uint64_t q, uint32_t* d_argmin,
                          float* d_min_or_null, rmq_stream_t stream);
 
+/* Bounds-checked builds only (librmq_gb300_checked.so, compiled with
+ * RMQ_DEBUG_BOUNDS=1): *count = level loads of the query kernels that fell
+ * outside their level since the last call on this device (each such load is
+ * skipped, not made), then the count is cleared.  The regular library
+ * returns RMQ_ERR_UNSUPPORTED. */
+int rmq_debug_bounds_violations(uint64_t* count);
+
 /* Level layout only (host computation, no device work): the reference's rule
  * (src/xxx.h:225-243) generalised to rf = 2^rf_log.  Returns RMQ_ERR_ARG when
  * t is below the variant's minimum.  Usable without a GPU. */

@@ -6,6 +6,7 @@ and the reference build, the host logic, and the C ABI's symbol table.
 """
 from __future__ import annotations
 
+import os
 import sys
 from pathlib import Path
 
@@ -24,6 +25,21 @@ GOLDEN = ROOT / "tests" / "golden"
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
     config.addinivalue_line("markers", "slow: full-size workload")
+
+
+def pytest_sessionfinish(session, exitstatus):
+    """In a run against the bounds-checked build (RMQ_EXPECT_CHECKED_LIB set,
+    RMQ_GB300_LIB naming librmq_gb300_checked.so): after the tests, read the
+    device-side count of out-of-level loads and fail the run unless it is 0."""
+    if not os.environ.get("RMQ_EXPECT_CHECKED_LIB") or exitstatus != 0:
+        return
+    import ctypes
+    import rmq_gb300 as R
+    count = ctypes.c_uint64()
+    st = R.lib().rmq_debug_bounds_violations(ctypes.byref(count))
+    print(f"\nbounds-checked build: status {st}, out-of-level loads {count.value}")
+    if st != R.RMQ_OK or count.value != 0:
+        session.exitstatus = 3
 
 
 @pytest.fixture(scope="session", autouse=True)

@@ -103,3 +103,11 @@ def test_bad_arguments_rejected_before_device_work():
     assert L.rmq_scan_bruteforce(0x1000, 10, 0x1004, 1, 0x2000, None, None) == R.RMQ_ERR_ARG
     assert L.rmq_get_info(None, None) == R.RMQ_ERR_ARG
     L.rmq_destroy(None)
+
+
+def test_regular_build_has_no_bounds_counter():
+    """Only the bounds-checked build counts out-of-level loads."""
+    count = ctypes.c_uint64(7)
+    assert R.lib().rmq_debug_bounds_violations(ctypes.byref(count)) == R.RMQ_ERR_UNSUPPORTED
+    assert count.value == 0
+    assert R.lib().rmq_debug_bounds_violations(None) == R.RMQ_ERR_ARG
