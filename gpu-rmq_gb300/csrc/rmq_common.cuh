@@ -123,6 +123,24 @@ __device__ __forceinline__ void ld_sector_policy(const float* p, float (&v)[8], 
 }
 
 // Eight consecutive uint32 (one 32-byte sector) with an L2 cache policy.
+// The same load, allocating in L1 (for the small top levels, which every SM
+// re-reads for many queries).
+__device__ __forceinline__ void ld_sector_l1_policy(const float* p, float (&v)[8], uint64_t pol) {
+    asm(
+        "ld.global.nc.L2::cache_hint.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8], %9;"
+        : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]),
+          "=f"(v[4]), "=f"(v[5]), "=f"(v[6]), "=f"(v[7])
+        : "l"(p), "l"(pol));
+}
+
+__device__ __forceinline__ void ld_sector_u32_l1_policy(const uint32_t* p, uint32_t (&v)[8], uint64_t pol) {
+    asm(
+        "ld.global.nc.L2::cache_hint.v8.u32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8], %9;"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]),
+          "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7])
+        : "l"(p), "l"(pol));
+}
+
 __device__ __forceinline__ void ld_sector_u32_policy(const uint32_t* p, uint32_t (&v)[8], uint64_t pol) {
     asm(
         "ld.global.nc.L1::no_allocate.L2::cache_hint.v8.u32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8], %9;"

@@ -61,7 +61,7 @@ __device__ __forceinline__ void cl_sector(const Levels& lv, uint32_t k, uint32_t
     const uint32_t jlo = s < lo ? lo - s : 0u;
     const uint32_t jhi = hi - s < 8u ? hi - s : 8u;
     float v[8];
-    load_level_sector(lv, k, s, pol, v);
+    load_level_sector<uint32_t, false>(lv, k, s, pol, v);
     const float sm = sector_min(v, jlo, jhi);
     if (ARGMIN) {
         if (sm < b.v || (sm == b.v && key < b.key)) {
@@ -169,7 +169,7 @@ query_cl_kernel(Levels lv, const uint2* __restrict__ qs, uint32_t q, float* __re
                 const uint32_t jlo = (b.meta >> 8) & 0xffu;
                 const uint32_t jhi = (b.meta >> 16) & 0xffu;
                 float v[8];
-                load_level_sector(lv, k, b.s, pol, v);
+                load_level_sector<uint32_t, false>(lv, k, b.s, pol, v);
                 uint32_t jj = jlo;
 #pragma unroll
                 for (int t = 7; t >= 0; --t)

@@ -73,9 +73,21 @@ __device__ __forceinline__ uint64_t ld_index(const uint64_t* p) {
 #endif
 }
 
+// Coarse levels of at most this many entries (64 KiB of values; with the
+// smaller levels above them at most ~73 KiB) are read through L1: every SM
+// re-reads these top levels for many queries, and a query that descends to
+// them otherwise pays an L2 round trip per level.  Larger levels, and level 0,
+// bypass L1.  Measured at n = q = 2^26: uniform-length queries 9.2 -> 23.7 G
+// queries/s, the three-way mixture 12.2 -> 20.8, the lognormal(2^13, 1)
+// workload +1.4 %; including the 2^17-entry level (512 KiB) cost 5 % on the
+// uniform law.  The stored indices of those levels (phase 2) likewise.  The
+// CL kernel keeps every level out of L1 (TOP_L1 = false): its tiles re-read
+// the same sectors from L2 lane by lane, and the extra branch cost it 2 %.
+constexpr uint32_t kL1LevelEntries = 1u << 14;
+
 // Loads the sector starting at s of level k.  Level 0 is the caller's array,
 // which is not padded: a sector that crosses its end is read element-wise.
-template <typename I>
+template <typename I, bool TOP_L1 = true>
 __device__ __forceinline__ void load_level_sector(const LevelsT<I>& lv, uint32_t k, I s,
                                                   const L2Policies& pol, float (&v)[8]) {
 #if RMQ_DEBUG_BOUNDS
@@ -89,7 +101,8 @@ __device__ __forceinline__ void load_level_sector(const LevelsT<I>& lv, uint32_t
 #endif
     const float* base = lv.val[k];
     if (k > 0) {
-        ld_sector_policy(base + s, v, pol.coarse);
+        if (TOP_L1 && lv.size[k] <= kL1LevelEntries) ld_sector_l1_policy(base + s, v, pol.coarse);
+        else ld_sector_policy(base + s, v, pol.coarse);
     } else if (s + 8u <= lv.size[0]) {
         ld_sector_policy(base + s, v, pol.fine);
     } else {
@@ -334,7 +347,10 @@ __device__ __forceinline__ void vl_locate(const LevelsT<I>& lv, I l, const Track
             for (int j = 0; j < 8; ++j) ix[j] = 0u;
         } else
 #endif
-        if (k > 0) ld_sector_u32_policy(lv.idx[k] + w.s, ix, pol.coarse);
+        if (k > 0) {
+            if (lv.size[k] <= kL1LevelEntries) ld_sector_u32_l1_policy(lv.idx[k] + w.s, ix, pol.coarse);
+            else ld_sector_u32_policy(lv.idx[k] + w.s, ix, pol.coarse);
+        }
     }
     uint32_t j = jlo;
 #pragma unroll
