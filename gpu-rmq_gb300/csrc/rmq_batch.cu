@@ -513,6 +513,24 @@ int rmq_batch_autotune(rmq_batch* b, rmq_stream_t stream, rmq_batch_info* info) 
     return info != nullptr ? rmq_batch_get_info(b, info) : RMQ_OK;
 }
 
+int rmq_batch_set_tuning(rmq_batch* b, uint64_t scan_threshold, uint32_t query_block, rmq_stream_t stream) {
+    if (b == nullptr || scan_threshold < 8 || query_block < 32 || query_block > rmq::kMaxQueryThreads ||
+        query_block % 32 != 0)
+        return RMQ_ERR_ARG;
+    DeviceGuard guard(b->device);
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    int st = plan(b, scan_threshold, s);  // RMQ_ERR_UNSUPPORTED when the levels would not fit
+    if (st != RMQ_OK) return st;
+    b->qblock = query_block;
+    if (b->queries_set) {
+        st = upload_blocks(b, s);
+        if (st != RMQ_OK) return st;
+    }
+    drop_graph(b);
+    b->build_timed = false;
+    return RMQ_OK;
+}
+
 int rmq_batch_get_info(const rmq_batch* bc, rmq_batch_info* info) {
     if (bc == nullptr || info == nullptr) return RMQ_ERR_ARG;
     rmq_batch* b = const_cast<rmq_batch*>(bc);

@@ -403,6 +403,7 @@ def _bind_batch() -> ctypes.CDLL:
             getattr(L, name).argtypes = [_P, _P]
         L.rmq_batch_autotune.argtypes = [_P, _P, ctypes.POINTER(BatchInfo)]
         L.rmq_batch_get_info.argtypes = [_P, ctypes.POINTER(BatchInfo)]
+        L.rmq_batch_set_tuning.argtypes = [_P, _U64, ctypes.c_uint32, _P]
         L.rmq_batch_destroy.argtypes = [_P]
         L.rmq_batch_destroy.restype = None
         L.rmq_gen_values_device.argtypes = [_P, _U64, _U64, _P]
@@ -434,6 +435,7 @@ class Batch:
     def set_queries(self, lr, query_offsets, out_idx=None, out_min=None, stream=None):
         qo = np.ascontiguousarray(query_offsets, dtype=np.uint64)
         self._keep = (lr, out_idx, out_min, qo)
+        self.query_offsets = qo
         st = _bind_batch().rmq_batch_set_queries(
             self._h, _dev_ptr(lr) if lr.numel() else None, qo.ctypes.data,
             _dev_ptr(out_idx) if out_idx is not None else None,
@@ -455,11 +457,45 @@ class Batch:
     def run(self, stream=None):
         self._call("rmq_batch_run", stream)
 
-    def autotune(self, stream=None) -> BatchInfo:
+    def set_tuning(self, t: int, query_block: int, stream=None) -> None:
+        """Applies a known (t, CTA size); rebuild before querying."""
+        st = _bind_batch().rmq_batch_set_tuning(self._h, int(t), int(query_block), _stream_handle(stream))
+        if st != RMQ_OK:
+            raise RMQError(st, "rmq_batch_set_tuning")
+
+    def workload_key(self) -> str:
+        """Identifies the tuning problem: the GPU, the array sizes and the
+        per-array query counts (the autotuner times exactly these)."""
+        import hashlib
+        import torch
+        hsh = hashlib.sha256()
+        hsh.update(torch.cuda.get_device_name(self.values.device).encode())
+        hsh.update(self.sizes.tobytes())
+        hsh.update(np.diff(getattr(self, "query_offsets", np.zeros(1, np.uint64))).astype(np.uint64).tobytes())
+        return hsh.hexdigest()[:32]
+
+    def autotune(self, stream=None, cache: str | os.PathLike | None = None) -> BatchInfo:
+        """Runs the autotuner, or, when `cache` (a JSON file) already holds a
+        choice for this workload (workload_key), applies it and rebuilds.  A
+        fresh choice is added to the cache."""
+        import json
+        key = self.workload_key() if cache is not None else None
+        table = {}
+        if cache is not None and Path(cache).exists():
+            table = json.loads(Path(cache).read_text())
+            hit = table.get(key)
+            if hit is not None:
+                self.set_tuning(hit["scan_threshold"], hit["query_block"], stream)
+                self.build(stream)
+                return self.info()
         info = BatchInfo()
         st = _bind_batch().rmq_batch_autotune(self._h, _stream_handle(stream), ctypes.byref(info))
         if st != RMQ_OK:
             raise RMQError(st, "rmq_batch_autotune")
+        if cache is not None:
+            table[key] = {"scan_threshold": int(info.scan_threshold), "query_block": int(info.query_block),
+                          "query_ms": float(info.query_ms), "arrays": self.num_arrays}
+            Path(cache).write_text(json.dumps(table, indent=1, sort_keys=True))
         return info
 
     def info(self) -> BatchInfo:

@@ -70,6 +70,13 @@ int rmq_batch_run(rmq_batch* b, rmq_stream_t stream);
  * Blocking.  The choice is reported in *info (may be NULL). */
 int rmq_batch_autotune(rmq_batch* b, rmq_stream_t stream, rmq_batch_info* info);
 
+/* Applies a known choice (for example one rmq_batch_autotune made earlier for
+ * the same workload): scan threshold t (>= 8) and CTA size (a multiple of 32,
+ * <= 512) of the query kernel.  The levels must be rebuilt (rmq_batch_build or
+ * rmq_batch_run) before querying.  RMQ_ERR_UNSUPPORTED when t would need more
+ * level storage than the batch holds (any t >= 16, or the creation t, fits). */
+int rmq_batch_set_tuning(rmq_batch* b, uint64_t scan_threshold, uint32_t query_block, rmq_stream_t stream);
+
 int rmq_batch_get_info(const rmq_batch* b, rmq_batch_info* info);
 
 /* Frees the batch's device memory and graph.  Safe on NULL. */

@@ -137,3 +137,48 @@ def test_device_generators(cuda):
             assert 0.8 * med < np.median(length) < 1.25 * med
         else:
             assert abs(np.mean(length) / n - 0.5) < 0.01
+
+
+def test_tuning_cache_and_set_tuning(cuda, tmp_path):
+    """A tuning choice stored in the JSON cache is applied (no tuning pass)
+    on the same workload and gives the same exact results; set_tuning checks
+    its arguments and the level capacity."""
+    import json
+    import torch
+    rng = np.random.default_rng(5)
+    sizes = [int(x) for x in np.exp(rng.uniform(np.log(1 << 10), np.log(1 << 18), 40))]
+    dv, dq, offs, arrays, qs, qo = _make_batch(cuda, sizes, 5)
+    emin, eidx = _expected(arrays, qs, qo)
+    q = qs.shape[0]
+    cache = tmp_path / "tuning.json"
+    out_min = torch.empty(q, dtype=torch.float32, device=cuda)
+    out_idx = torch.empty(q, dtype=torch.int32, device=cuda)
+    with R.Batch(dv, offs, sizes, t=64) as b:
+        b.set_queries(dq, qo, out_idx, out_min)
+        first = b.autotune(cache=cache)
+        table = json.loads(cache.read_text())
+        assert list(table.values())[0]["scan_threshold"] == first.scan_threshold
+        key = b.workload_key()
+    # pretend an earlier run chose (t = 1024, 256 threads): the cache is applied as is
+    table[key] = {"scan_threshold": 1024, "query_block": 256, "query_ms": 1.0, "arrays": len(sizes)}
+    cache.write_text(json.dumps(table))
+    with R.Batch(dv, offs, sizes, t=64) as b:
+        b.set_queries(dq, qo, out_idx, out_min)
+        info = b.autotune(cache=cache)
+        assert info.scan_threshold == 1024 and info.query_block == 256
+        out_min.fill_(-1)
+        out_idx.fill_(-1)
+        b.run()
+        torch.cuda.synchronize()
+        _check(out_min, out_idx, emin, eidx, "cached tuning")
+        for bad_t, bad_block in ((4, 128), (64, 48), (64, 1024)):
+            with pytest.raises(R.RMQError) as e:
+                b.set_tuning(bad_t, bad_block)
+            assert e.value.status == R.RMQ_ERR_ARG
+        with pytest.raises(R.RMQError) as e:
+            b.set_tuning(8, 128)  # deeper than the levels allocated for t >= 16
+        assert e.value.status == R.RMQ_ERR_UNSUPPORTED
+        b.set_tuning(32, 512)
+        b.run()
+        torch.cuda.synchronize()
+        _check(out_min, out_idx, emin, eidx, "set_tuning(32, 512)")
