@@ -141,11 +141,13 @@ query_cl_kernel(Levels lv, const uint2* __restrict__ qs, uint32_t q, float* __re
         for (int o = 1; o < G; o <<= 1) m = fminf(m, __shfl_xor_sync(mask, m, o, G));
         bool locate = ARGMIN;
         if (!ARGMIN) {
-            if (m != 0.0f) {
+            // A +0.0 minimum means no -0.0 in the range (min.f32 returns -0.0
+            // whenever one meets a zero): only -0.0 needs the first zero's bits.
+            if (__float_as_uint(m) != 0x80000000u) {
                 if (lane == j) st_stream(out_min + base + j, m);
                 continue;
             }
-            // A zero minimum may be -0.0 or +0.0: locate the first one for its bits.
+            // A -0.0 minimum: locate the first zero for its bits.
             b = LaneBest{f_inf(), kKeyNone, 0u, 0u};
             cl_query<R, G, true>(lv, l, r, lane, pol, b);
             locate = true;

@@ -399,8 +399,12 @@ __device__ __forceinline__ bool vl_compute(const LevelsT<I>& lv, typename IdxTra
     } else {
         float m = vl_phase1<R, false>(lv, valid, l, r, pol, tl, tr);
         // A zero minimum may be -0.0 or +0.0; the reference returns the bits of
-        // the first occurrence, so locate it (warp-uniform participation).
-        const bool zero = valid && m == 0.0f;
+        // the first occurrence.  min.f32 returns -0.0 whenever a -0.0 meets a
+        // zero (checked on sm_103a, and by the signed-zero parity cases), so a
+        // +0.0 minimum means the range holds no -0.0 and is already the answer;
+        // only a -0.0 minimum needs the first zero located (warp-uniform
+        // participation).
+        const bool zero = valid && __float_as_uint(m) == 0x80000000u;
         if (__any_sync(0xffffffffu, zero)) {
             vl_phase1<R, true>(lv, zero, l, r, pol, tl, tr);
             if (zero) vl_locate<R>(lv, l, tl, tr, pol, m, idx);

@@ -116,6 +116,13 @@ def test_special_values(cuda, cfg):
         "all_equal": np.full(n, 0.5, np.float32),
         "all_inf": np.full(n, np.inf, np.float32),
         "zeros_mixed": np.where(rng.random(n) < 0.5, -0.0, 0.0).astype(np.float32),
+        # sparse zeros among positives: +0.0 before -0.0, -0.0 before +0.0, one sign only
+        "zeros_plus_first": np.where(np.arange(n) % 97 == 5, np.where(np.arange(n) < n // 2, 0.0, -0.0),
+                                     1.0 + rng.random(n)).astype(np.float32),
+        "zeros_minus_first": np.where(np.arange(n) % 97 == 5, np.where(np.arange(n) < n // 2, -0.0, 0.0),
+                                      1.0 + rng.random(n)).astype(np.float32),
+        "zeros_plus_only": np.where(np.arange(n) % 211 == 7, 0.0, 1.0 + rng.random(n)).astype(np.float32),
+        "zeros_minus_only": np.where(np.arange(n) % 211 == 7, -0.0, 1.0 + rng.random(n)).astype(np.float32),
         "neg": (-rng.random(n)).astype(np.float32),
         "descending": np.arange(n, 0, -1).astype(np.float32),
     }
