@@ -8,9 +8,14 @@ query returns its fp32 minimum and its int32 argmin (ties to the lowest
 index).  One step is one pass of the query kernel over all q queries with the
 array, the hierarchy and the queries resident in HBM.  The inputs (1 GiB of
 queries and values, 512 MiB of outputs) exceed the 129 MB L2, so no flush is
-needed between steps.
+needed between steps (smaller workloads, --n / --q, are timed step by step
+with L2 flushed in between).  The line also carries the roofline of the
+query kernel, the end-to-end figure through rmq_query_idx_host on page-locked
+host buffers, the reference's own GPU kernels timed on the same inputs, the
+CPU baseline and the SM clocks sampled during the timed region.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--mode plain|batched|serve] [--n N --q Q --lr L --t T --ties F]
 
 Under torchrun each rank builds and queries its own replica on its own GPU
 (no collective on the data path); value = all ranks' queries / max-over-ranks
