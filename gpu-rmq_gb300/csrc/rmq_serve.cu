@@ -30,6 +30,7 @@
 #include <mutex>
 #include <new>
 #include <thread>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/rmq_gb300_batch.h"
@@ -135,7 +136,10 @@ struct rmq_server {
     uint8_t* arena = nullptr;
     Arena alloc;
     std::vector<ServedArray> arrays;
-    std::deque<Request> requests;
+    // Requests by id, kept until their waiter has collected the outcome (or
+    // the server is destroyed); unordered_map keeps element addresses stable.
+    std::unordered_map<uint64_t, Request> requests;
+    uint64_t next_request = 0;
     std::deque<uint64_t> pending;
     std::vector<uint64_t> admitting;
     std::vector<Slot> slots;
@@ -269,7 +273,7 @@ bool launch_batch(rmq_server* s, Slot& sl, std::unique_lock<std::mutex>& lk) {
     sl.rptr.clear();
     sl.req_off.clear();
     for (auto it = s->pending.begin(); it != s->pending.end() && sl.reqs.size() < max_r;) {
-        Request& r = s->requests[*it];
+        Request& r = s->requests.at(*it);
         ServedArray& a = s->arrays[r.array];
         if (!a.resident && !admit(s, r.array)) {
             ++it;  // waits for memory to free up
@@ -397,7 +401,7 @@ void dispatcher_main(rmq_server* s) {
             // Stopping: requests that can never be admitted are failed.
             if (!s->pending.empty() && s->admitting.empty() && !progressed) {
                 for (uint64_t rid : s->pending) {
-                    Request& r = s->requests[rid];
+                    Request& r = s->requests.at(rid);
                     r.status = RMQ_ERR_OOM;
                     r.done = true;
                     r.t_done = Clock::now();
@@ -521,8 +525,8 @@ int rmq_server_submit(rmq_server* s, uint64_t array_id, const uint32_t* h_lr, ui
     r.h_idx = h_argmin;
     r.h_min = h_min;
     r.t_submit = Clock::now();
-    *request_id = s->requests.size();
-    s->requests.push_back(r);
+    *request_id = s->next_request++;
+    s->requests.emplace(*request_id, r);
     s->pending.push_back(*request_id);
     s->not_done++;
     s->cv_work.notify_one();
@@ -532,14 +536,17 @@ int rmq_server_submit(rmq_server* s, uint64_t array_id, const uint32_t* h_lr, ui
 int rmq_server_wait(rmq_server* s, uint64_t request_id, int64_t timeout_ms, double* latency_us) {
     if (s == nullptr) return RMQ_ERR_ARG;
     std::unique_lock<std::mutex> lk(s->mu);
-    if (request_id >= s->requests.size()) return RMQ_ERR_ARG;
-    auto done = [&] { return s->requests[request_id].done; };
+    auto it = s->requests.find(request_id);
+    if (it == s->requests.end()) return RMQ_ERR_ARG;  // unknown, or already collected
+    const Request& r = it->second;
+    auto done = [&] { return r.done; };
     if (timeout_ms < 0) s->cv_done.wait(lk, done);
     else if (!s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), done)) return RMQ_ERR_TIMEOUT;
-    const Request& r = s->requests[request_id];
     if (latency_us != nullptr)
         *latency_us = std::chrono::duration<double, std::micro>(r.t_done - r.t_submit).count();
-    return r.status;
+    const int status = r.status;
+    s->requests.erase(it);  // collected: the id is no longer valid
+    return status;
 }
 
 int rmq_server_drain(rmq_server* s, int64_t timeout_ms) {
@@ -583,10 +590,16 @@ int rmq_server_replay(rmq_server* s, const rmq_trace_event* ev, uint64_t count, 
             if (latency_us) latency_us[i] = -1.0;
             continue;
         }
-        const Request& r = s->requests[rid[i]];
+        auto it = s->requests.find(rid[i]);
+        if (it == s->requests.end()) {
+            if (latency_us) latency_us[i] = -1.0;
+            continue;
+        }
+        const Request& r = it->second;
         if (latency_us) latency_us[i] = std::chrono::duration<double, std::micro>(r.t_done - r.t_submit).count();
         if (r.t_submit < first) first = r.t_submit;
         if (r.t_done > last) last = r.t_done;
+        s->requests.erase(it);  // the replay collects its own requests
     }
     if (wall_s) *wall_s = first == Clock::time_point::max() ? 0.0 : std::chrono::duration<double>(last - first).count();
     return st;

@@ -81,7 +81,10 @@ int rmq_server_submit(rmq_server* s, uint64_t array_id, const uint32_t* h_lr, ui
 /* Waits for a request: its status (RMQ_OK, or RMQ_ERR_QUERY_RANGE when a
  * query was invalid), or RMQ_ERR_TIMEOUT when it is not done within
  * timeout_ms (< 0: no limit).  *latency_us (may be NULL): submit to results
- * in the host buffers. */
+ * in the host buffers.  A call that returns the status collects the request:
+ * the server drops its record and the id is then unknown (RMQ_ERR_ARG);
+ * records of requests that are never waited for are kept until
+ * rmq_server_destroy. */
 int rmq_server_wait(rmq_server* s, uint64_t request_id, int64_t timeout_ms, double* latency_us);
 
 /* Waits until every submitted request is done (RMQ_ERR_TIMEOUT otherwise). */

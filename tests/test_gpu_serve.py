@@ -93,9 +93,11 @@ def test_invalid_query_and_replay(cuda):
         qs = np.array([[0, 999], [10, 5], [0, 1000]], dtype=np.uint32)
         oi = np.empty(3, np.uint32)
         om = np.empty(3, np.float32)
-        st, _ = srv.wait(srv.submit(aid, qs, oi, om))
+        rid = srv.submit(aid, qs, oi, om)
+        st, _ = srv.wait(rid)
         assert st == R.RMQ_ERR_QUERY_RANGE
         assert oi[0] == np.argmin(a) and oi[1] == R.NO_POS and oi[2] == R.NO_POS and np.isnan(om[1])
+        assert srv.wait(rid)[0] == R.RMQ_ERR_ARG  # collected by the first wait
         # a small replayed stream: a registration and requests before and after it
         lr = _queries(rng, 1000, 3000)
         ev = np.zeros(4, dtype=R.TRACE_DTYPE)
