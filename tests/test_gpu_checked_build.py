@@ -21,7 +21,7 @@ pytestmark = pytest.mark.gpu
 
 ROOT = Path(__file__).resolve().parents[1]
 CHECKED = ROOT / "gpu-rmq_gb300" / "librmq_gb300_checked.so"
-SUITES = ["tests/test_gpu_parity.py", "tests/test_gpu_wide.py", "tests/test_gpu_batch.py",
+SUITES = ["tests/test_gpu_parity.py", "tests/test_gpu_fuzz.py", "tests/test_gpu_wide.py", "tests/test_gpu_batch.py",
           "tests/test_gpu_host_buffers.py", "tests/test_gpu_serve.py", "tests/test_zz_no_alloc.py"]
 
 
