@@ -23,6 +23,7 @@ struct rmq_handle {
     float* val_buf = nullptr;
     uint32_t* idx_buf = nullptr;
     uint64_t* idx_buf64 = nullptr;  // 64-bit handles
+    unsigned* counters = nullptr;   // arrival counters of the single-launch build (after the levels)
     bool wide = false;
     uint32_t* err = nullptr;  // invalid-query counter (validate mode)
     int device = 0;
@@ -226,9 +227,15 @@ int rmq_build(const float* d_values, uint64_t n, const rmq_config* cfg, rmq_stre
         // One allocation: level values, then argmin indices, so that a single
         // L2 access-policy window can cover both.
         const size_t idx_bytes = h->with_index ? (wide ? sizeof(uint64_t) : sizeof(uint32_t)) : 0;
-        e = cudaMalloc(&h->val_buf, h->lay.total * (sizeof(float) + idx_bytes));
+        const size_t level_bytes = h->lay.total * (sizeof(float) + idx_bytes);
+        const size_t counter_bytes = rmq::tail_counters(h->lay) * sizeof(unsigned);
+        e = cudaMalloc(&h->val_buf, level_bytes + counter_bytes);
         if (e == cudaSuccess && h->with_index && !wide) h->idx_buf = reinterpret_cast<uint32_t*>(h->val_buf + h->lay.total);
         if (e == cudaSuccess && h->with_index && wide) h->idx_buf64 = reinterpret_cast<uint64_t*>(h->val_buf + h->lay.total);
+        if (e == cudaSuccess && counter_bytes > 0) {
+            h->counters = reinterpret_cast<unsigned*>(reinterpret_cast<char*>(h->val_buf) + level_bytes);
+            e = cudaMemsetAsync(h->counters, 0, counter_bytes, s);
+        }
     }
     if (e == cudaSuccess) e = cudaMalloc(&h->err, sizeof(uint32_t));
     if (e != cudaSuccess) {
@@ -242,8 +249,8 @@ int rmq_build(const float* d_values, uint64_t n, const rmq_config* cfg, rmq_stre
     if (e == cudaSuccess) e = cudaEventCreate(&e1);
     if (e == cudaSuccess) e = cudaEventRecord(e0, s);
     if (e == cudaSuccess)
-        e = wide ? rmq::launch_build64(h->lay, d_values, h->val_buf, h->idx_buf64, s)
-                 : rmq::launch_build(h->lay, d_values, h->val_buf, h->idx_buf, s);
+        e = wide ? rmq::launch_build64(h->lay, d_values, h->val_buf, h->idx_buf64, s, h->counters)
+                 : rmq::launch_build(h->lay, d_values, h->val_buf, h->idx_buf, s, h->counters);
     if (e == cudaSuccess) e = cudaEventRecord(e1, s);
     if (e == cudaSuccess) e = cudaEventSynchronize(e1);
     if (e == cudaSuccess) e = cudaEventElapsedTime(&h->build_ms, e0, e1);

@@ -4,7 +4,9 @@
 // rf source entries to one minimum with a cooperative-groups tile, one launch
 // per level (src/xxx.h:258-265).  Here the levels whose blocks fit in an
 // 8192-entry tile are built by one fused streaming kernel (level 0 is read
-// once), and the small levels above by a single-CTA tail kernel.  Every block
+// once), and the small levels above by a single-CTA tail kernel, or, for up
+// to kInKernelTailMaxTiles tiles, inside the fused kernel itself
+// (tail_upward: the tile completing a group computes the group's entry).  Every block
 // stores its first-occurring minimum and that entry's level-0 index, which
 // argmin queries use.  build_step_kernel (one level step, rf/8 lanes per
 // block) covers large intermediate levels of very large arrays.
@@ -95,10 +97,11 @@ Layout plan_layout(uint64_t n, uint64_t t, uint32_t rf_log) {
 // ---------------------------------------------------------------------------
 template <int R, typename P>
 __global__ void __launch_bounds__(kFusedThreads)
-build_fused_kernel(const float* __restrict__ a, P n, LevelOutT<P> out, uint32_t depth) {
+build_fused_kernel(const float* __restrict__ a, P n, LevelOutT<P> out, uint32_t depth, TailPlan tp) {
     __shared__ float sv[kTileSectors];
     __shared__ P sp[kTileSectors];
     fused_tile<R>(a, n, out, depth, blockIdx.x, sv, sp);
+    if (tp.top > tp.depth) tail_upward<R>(out, tp, blockIdx.x);
 }
 
 template <int R, typename P>
@@ -131,9 +134,26 @@ int build_launch_count(const Layout& lay) {
     }
 }
 
+// The in-kernel tail pays per tile (a fence and an atomic each, and a warp
+// of every tile that completes a group staying on for the parent's entry);
+// it wins over the two extra launches up to about a thousand tiles (n up to
+// 2^23: 18.3 -> 15 us at n = 2^20, t = 64; 24.5 -> 21.7 us at n = 2^23) and
+// loses beyond (70 -> 75 us at n = 2^26, 230 -> 261 us at n = 2^28).
+constexpr uint32_t kInKernelTailMaxTiles = 1024;
+
+uint64_t tail_counters(const Layout& lay) {
+    if (lay.num_levels < 2 || lay.rf_log < 3 || lay.rf_log > 5) return 0;
+    const uint32_t top = lay.num_levels - 1;
+    const uint32_t fd = 13u / lay.rf_log;  // fused_depth<R>()
+    const uint32_t depth = top < fd ? top : fd;
+    uint64_t c = 0;
+    for (uint32_t k = depth + 1; k <= top; ++k) c += lay.size[k];
+    return c;
+}
+
 template <int R, typename P>
 static cudaError_t build_levels(const Layout& lay, const float* d_values, float* val_buf, P* idx_buf,
-                                cudaStream_t s) {
+                                cudaStream_t s, unsigned* counters) {
     constexpr uint32_t LPB = (1u << R) / 8u;
     if (lay.num_levels < 2) return cudaSuccess;
     LevelOutT<P> out;
@@ -154,9 +174,22 @@ static cudaError_t build_levels(const Layout& lay, const float* d_values, float*
     plan_launches<R>(lay, &fused, &steps, &tail);
     const P n = P(lay.size[0]);
     const uint32_t tiles = uint32_t((uint64_t(n) + kTile - 1) / kTile);
-    build_fused_kernel<R, P><<<tiles, kFusedThreads, 0, s>>>(d_values, n, out, fused);
+    TailPlan tp = {};
+    tp.depth = fused;
+    tp.top = fused;  // no tail inside the kernel
+    if (counters != nullptr && fused + 1 < lay.num_levels && tiles <= kInKernelTailMaxTiles) {
+        tp.top = lay.num_levels - 1;
+        tp.per_tile = kTile >> (uint32_t(R) * fused);
+        tp.counters = counters;
+        uint64_t c = 0;
+        for (uint32_t k = fused + 1; k <= tp.top; ++k) {
+            tp.coff[k] = c;
+            c += lay.size[k];
+        }
+    }
+    build_fused_kernel<R, P><<<tiles, kFusedThreads, 0, s>>>(d_values, n, out, fused, tp);
     cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
+    if (e != cudaSuccess || tp.top > tp.depth) return e;
     uint32_t k = fused;
     for (uint32_t i = 0; i < steps; ++i, ++k) {
         const P dst_size = out.size[k + 1];
@@ -176,23 +209,23 @@ static cudaError_t build_levels(const Layout& lay, const float* d_values, float*
 
 template <typename P>
 static cudaError_t launch_build_p(const Layout& lay, const float* d_values, float* val_buf, P* idx_buf,
-                                  cudaStream_t s) {
+                                  cudaStream_t s, unsigned* counters) {
     switch (lay.rf_log) {
-        case 3: return build_levels<3, P>(lay, d_values, val_buf, idx_buf, s);
-        case 4: return build_levels<4, P>(lay, d_values, val_buf, idx_buf, s);
-        case 5: return build_levels<5, P>(lay, d_values, val_buf, idx_buf, s);
+        case 3: return build_levels<3, P>(lay, d_values, val_buf, idx_buf, s, counters);
+        case 4: return build_levels<4, P>(lay, d_values, val_buf, idx_buf, s, counters);
+        case 5: return build_levels<5, P>(lay, d_values, val_buf, idx_buf, s, counters);
         default: return cudaErrorInvalidValue;
     }
 }
 
 cudaError_t launch_build(const Layout& lay, const float* d_values, float* val_buf,
-                         uint32_t* idx_buf, cudaStream_t s) {
-    return launch_build_p<uint32_t>(lay, d_values, val_buf, idx_buf, s);
+                         uint32_t* idx_buf, cudaStream_t s, unsigned* counters) {
+    return launch_build_p<uint32_t>(lay, d_values, val_buf, idx_buf, s, counters);
 }
 
 cudaError_t launch_build64(const Layout& lay, const float* d_values, float* val_buf,
-                           uint64_t* idx_buf, cudaStream_t s) {
-    return launch_build_p<uint64_t>(lay, d_values, val_buf, idx_buf, s);
+                           uint64_t* idx_buf, cudaStream_t s, unsigned* counters) {
+    return launch_build_p<uint64_t>(lay, d_values, val_buf, idx_buf, s, counters);
 }
 
 }  // namespace rmq

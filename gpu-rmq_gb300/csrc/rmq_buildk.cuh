@@ -143,6 +143,88 @@ __device__ __forceinline__ void fused_tile(const float* __restrict__ a, P n, con
     }
 }
 
+// Levels above the fused tiles, built inside the fused kernel.  Entry g of
+// level k depends on the tiles (k = depth + 1) or entries of level k - 1
+// (k > depth + 1) below it; each of those, when done, adds one arrival to
+// g's counter, and the last arrival computes g (one warp: a lane per child,
+// first-occurrence reduction) and passes on to g's parent.  No CTA waits:
+// whoever completes a group does its work.  Every counter is reset by its
+// last arrival, so the counters are all zero again after the build.
+struct TailPlan {
+    uint32_t depth;     // top level built inside the tiles
+    uint32_t top;       // top level of the hierarchy (> depth when there is a tail)
+    uint32_t per_tile;  // level-`depth` entries per tile
+    unsigned* counters;
+    uint64_t coff[kMaxLevels];  // first counter of level k, depth < k <= top
+};
+
+template <typename P>
+__device__ __forceinline__ P ldcg_pos(const P* p);
+template <>
+__device__ __forceinline__ uint32_t ldcg_pos(const uint32_t* p) { return __ldcg(p); }
+template <>
+__device__ __forceinline__ uint64_t ldcg_pos(const uint64_t* p) {
+    return __ldcg(reinterpret_cast<const unsigned long long*>(p));
+}
+
+template <int R, typename P>
+__device__ __forceinline__ void tail_upward(const LevelOutT<P>& out, const TailPlan& tp, uint64_t tile) {
+    constexpr uint32_t RF = 1u << R;
+    constexpr P kNone = IdxTraits<P>::none;
+    __shared__ unsigned s_go;
+    __threadfence();  // this tile's level entries before its arrival
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const uint64_t g = (tile * tp.per_tile) >> R;
+        const uint64_t lo = g << R;
+        const uint64_t hi = lo + RF < uint64_t(out.size[tp.depth]) ? lo + RF : uint64_t(out.size[tp.depth]);
+        const unsigned expect = unsigned((hi - 1) / tp.per_tile - lo / tp.per_tile + 1);
+        unsigned* c = tp.counters + tp.coff[tp.depth + 1] + g;
+        const unsigned last = atomicAdd(c, 1u) + 1u == expect;
+        if (last) *c = 0u;
+        s_go = last;
+    }
+    __syncthreads();
+    if (s_go == 0u || threadIdx.x >= 32) return;
+    const uint32_t lane = threadIdx.x;
+    uint64_t g = (tile * tp.per_tile) >> R;
+    for (uint32_t k = tp.depth + 1;; ++k) {
+        __threadfence();  // the children's writers fenced before arriving
+        const uint64_t child = (g << R) + lane;
+        float v = f_inf();
+        P p = kNone;
+        if (lane < RF && child < uint64_t(out.size[k - 1])) {
+            v = __ldcg(out.val[k - 1] + child);
+            p = out.idx[k - 1] != nullptr ? ldcg_pos(out.idx[k - 1] + child) : P(child);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float ov = __shfl_xor_sync(0xffffffffu, v, o);
+            const P op = __shfl_xor_sync(0xffffffffu, p, o);
+            if (op != kNone && (p == kNone || ov < v || (ov == v && op < p))) {
+                v = ov;
+                p = op;
+            }
+        }
+        unsigned go = 0u;
+        if (lane == 0) {
+            out.val[k][g] = v;
+            if (out.idx[k] != nullptr) out.idx[k][g] = p;
+            if (k < tp.top) {
+                __threadfence();
+                const uint64_t gg = g >> R;
+                const uint64_t left = uint64_t(out.size[k]) - (gg << R);
+                const unsigned expect = unsigned(left < RF ? left : RF);
+                unsigned* c = tp.counters + tp.coff[k + 1] + gg;
+                go = atomicAdd(c, 1u) + 1u == expect;
+                if (go) *c = 0u;
+            }
+        }
+        if (k == tp.top || __shfl_sync(0xffffffffu, go, 0) == 0u) return;
+        g >>= R;
+    }
+}
+
 // Single CTA: builds levels from+1 .. last from level `from` (already built),
 // level after level, with a block barrier between levels (global writes of
 // the block are visible to it after __syncthreads).

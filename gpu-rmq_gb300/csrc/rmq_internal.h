@@ -24,12 +24,17 @@ Layout plan_layout(uint64_t n, uint64_t t, uint32_t rf_log);
 
 // Build level k+1 from level k for every k in [0, num_levels-1).
 // `val_buf`/`idx_buf` are the level buffers (layout.total entries each);
-// `idx_buf` may be null (no argmin support).
+// `idx_buf` may be null (no argmin support).  With `counters` (at least
+// tail_counters(lay) zeroed entries, left zeroed by every build, never used
+// by two builds at once) the levels above the fused tiles are built inside
+// the fused kernel (one launch in all); without, by extra launches.
 cudaError_t launch_build(const Layout& lay, const float* d_values, float* val_buf,
-                         uint32_t* idx_buf, cudaStream_t s);
+                         uint32_t* idx_buf, cudaStream_t s, unsigned* counters = nullptr);
 // Same with 64-bit positions (arrays beyond 2^32 entries).
 cudaError_t launch_build64(const Layout& lay, const float* d_values, float* val_buf,
-                           uint64_t* idx_buf, cudaStream_t s);
+                           uint64_t* idx_buf, cudaStream_t s, unsigned* counters = nullptr);
+// Arrival counters the single-launch build needs for `lay` (0: none).
+uint64_t tail_counters(const Layout& lay);
 
 struct QueryArgs {
     Levels lv;
