@@ -10,9 +10,9 @@
 // results into the requests' host buffers, unpins arrays, wakes waiters),
 // marks admitted arrays ready when their build event completes, and whenever
 // a slot is free packs the pending requests whose arrays are ready (FIFO, up
-// to max_batch_queries) into it and launches: H2D queries + descriptors,
+// to max_batch_queries) into it and launches: one H2D of descriptors + queries,
 // owner fill, one query kernel (the batched per-warp kernel, one descriptor
-// per request), D2H results, event.  Requests arriving while batches run are
+// per request), one D2H of the results, event.  Requests arriving while batches run are
 // admitted into the next free slot, so up to S batches overlap on the device
 // with builds of newly admitted arrays on their own stream.
 //
@@ -112,14 +112,13 @@ struct Request {
 struct Slot {
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
-    uint32_t* h_q = nullptr;   // pinned, 2 x max_q
-    uint32_t* h_idx = nullptr;  // pinned, max_q
-    float* h_min = nullptr;     // pinned, max_q
-    uint8_t* h_hdr = nullptr;   // pinned: descs | q_off | unit_off
-    uint32_t* d_q = nullptr;
-    uint32_t* d_idx = nullptr;
-    float* d_min = nullptr;
-    uint8_t* d_hdr = nullptr;
+    // One upload and one download per batch: in = descs | q_off | unit_off |
+    // queries (sized by the batch); out = argmin[nq] | min[nq].
+    uint8_t* h_in = nullptr;   // pinned
+    uint8_t* h_out = nullptr;  // pinned
+    uint8_t* d_in = nullptr;
+    uint8_t* d_out = nullptr;
+    uint64_t nq = 0;           // queries of the batch in flight
     uint32_t* d_owner = nullptr;
     std::vector<uint64_t> reqs;
     std::vector<Request*> rptr;     // stable element pointers (taken under the lock)
@@ -127,8 +126,10 @@ struct Slot {
     bool busy = false;
 };
 
-size_t header_bytes(uint32_t max_req) {
-    return size_t(max_req) * sizeof(rmq::ArrayDesc) + 2 * size_t(max_req + 1) * sizeof(uint64_t);
+// Bytes of a batch's header for nr requests, rounded to 16 (the queries follow).
+size_t header_bytes(uint32_t nr) {
+    const size_t b = size_t(nr) * sizeof(rmq::ArrayDesc) + 2 * size_t(nr + 1) * sizeof(uint64_t);
+    return (b + 15) & ~size_t(15);
 }
 
 }  // namespace
@@ -233,13 +234,15 @@ bool admit(rmq_server* s, uint64_t id) {
 // without mu held (the slot and its requests belong to the dispatcher).
 void finish_slot(rmq_server* s, Slot& sl) {
     std::vector<int> status(sl.reqs.size(), RMQ_OK);
+    const uint32_t* h_idx = reinterpret_cast<const uint32_t*>(sl.h_out);
+    const float* h_min = reinterpret_cast<const float*>(sl.h_out + sl.nq * sizeof(uint32_t));
     for (size_t i = 0; i < sl.reqs.size(); ++i) {
         Request& r = *sl.rptr[i];
         const uint64_t o = sl.req_off[i];
-        if (r.h_idx != nullptr) std::memcpy(r.h_idx, sl.h_idx + o, r.q * sizeof(uint32_t));
-        if (r.h_min != nullptr) std::memcpy(r.h_min, sl.h_min + o, r.q * sizeof(float));
+        if (r.h_idx != nullptr) std::memcpy(r.h_idx, h_idx + o, r.q * sizeof(uint32_t));
+        if (r.h_min != nullptr) std::memcpy(r.h_min, h_min + o, r.q * sizeof(float));
         for (uint64_t j = 0; j < r.q; ++j) {
-            if (sl.h_idx[o + j] == rmq::kNoPos) {
+            if (h_idx[o + j] == rmq::kNoPos) {
                 status[i] = RMQ_ERR_QUERY_RANGE;
                 break;
             }
@@ -307,24 +310,28 @@ bool launch_batch(rmq_server* s, Slot& sl, std::unique_lock<std::mutex>& lk) {
     for (uint32_t i = 0; i < nr; ++i) descs[i] = describe(s->arrays[reqs[i]->array]);
     lk.unlock();
 
-    // Header: descriptors | q_off[nr + 1] | unit_off[nr + 1]
-    rmq::ArrayDesc* hd = reinterpret_cast<rmq::ArrayDesc*>(sl.h_hdr);
-    uint64_t* hq = reinterpret_cast<uint64_t*>(sl.h_hdr + size_t(max_r) * sizeof(rmq::ArrayDesc));
-    uint64_t* hu = hq + (max_r + 1);
+    // Upload: descriptors | q_off[nr + 1] | unit_off[nr + 1] | queries.
+    const size_t hdr = header_bytes(nr);
+    rmq::ArrayDesc* hd = reinterpret_cast<rmq::ArrayDesc*>(sl.h_in);
+    uint64_t* hq = reinterpret_cast<uint64_t*>(sl.h_in + size_t(nr) * sizeof(rmq::ArrayDesc));
+    uint64_t* hu = hq + (nr + 1);
+    uint32_t* h_q = reinterpret_cast<uint32_t*>(sl.h_in + hdr);
     std::memcpy(hd, descs.data(), nr * sizeof(rmq::ArrayDesc));
     hq[0] = 0;
     hu[0] = 0;
     for (uint32_t i = 0; i < nr; ++i) {
-        std::memcpy(sl.h_q + 2 * sl.req_off[i], reqs[i]->h_lr, reqs[i]->q * 2 * sizeof(uint32_t));
+        std::memcpy(h_q + 2 * sl.req_off[i], reqs[i]->h_lr, reqs[i]->q * 2 * sizeof(uint32_t));
         hq[i + 1] = hq[i] + reqs[i]->q;
         hu[i + 1] = hu[i] + (reqs[i]->q + 31) / 32;
     }
-    const rmq::ArrayDesc* dd = reinterpret_cast<const rmq::ArrayDesc*>(sl.d_hdr);
-    const uint64_t* dq = reinterpret_cast<const uint64_t*>(sl.d_hdr + size_t(max_r) * sizeof(rmq::ArrayDesc));
-    const uint64_t* du = dq + (max_r + 1);
-    cudaError_t e = cudaMemcpyAsync(sl.d_q, sl.h_q, nq * 2 * sizeof(uint32_t), cudaMemcpyHostToDevice, sl.stream);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(sl.d_hdr, sl.h_hdr, header_bytes(max_r), cudaMemcpyHostToDevice, sl.stream);
+    const rmq::ArrayDesc* dd = reinterpret_cast<const rmq::ArrayDesc*>(sl.d_in);
+    const uint64_t* dq = reinterpret_cast<const uint64_t*>(sl.d_in + size_t(nr) * sizeof(rmq::ArrayDesc));
+    const uint64_t* du = dq + (nr + 1);
+    sl.nq = nq;
+    uint32_t* d_idx = reinterpret_cast<uint32_t*>(sl.d_out);
+    float* d_min = reinterpret_cast<float*>(sl.d_out + nq * sizeof(uint32_t));
+    cudaError_t e = cudaMemcpyAsync(sl.d_in, sl.h_in, hdr + nq * 2 * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                                    sl.stream);
     if (e == cudaSuccess) e = rmq::launch_fill_owner(du, nr, sl.d_owner, sl.stream);
     if (e == cudaSuccess) {
         rmq::BatchQueryArgs a;
@@ -336,23 +343,20 @@ bool launch_batch(rmq_server* s, Slot& sl, std::unique_lock<std::mutex>& lk) {
         a.total_units = hu[nr];
         a.lvl_val = reinterpret_cast<const float*>(s->arena);
         a.lvl_idx = reinterpret_cast<const uint32_t*>(s->arena);
-        a.qs = reinterpret_cast<const uint2*>(sl.d_q);
-        a.out_min = sl.d_min;
-        a.out_idx = sl.d_idx;
+        a.qs = reinterpret_cast<const uint2*>(sl.d_in + hdr);
+        a.out_min = d_min;
+        a.out_idx = d_idx;
         a.threads = s->cfg.query_threads;
         e = rmq::launch_batch_query(a, sl.stream);
     }
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(sl.h_idx, sl.d_idx, nq * sizeof(uint32_t), cudaMemcpyDeviceToHost, sl.stream);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(sl.h_min, sl.d_min, nq * sizeof(float), cudaMemcpyDeviceToHost, sl.stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(sl.h_out, sl.d_out, nq * 8, cudaMemcpyDeviceToHost, sl.stream);
     if (e == cudaSuccess) e = cudaEventRecord(sl.done, sl.stream);
     if (e != cudaSuccess) {
         // Launch failure: fail the batch's requests (results undefined).
         cudaGetLastError();
         cudaStreamSynchronize(sl.stream);
         for (uint32_t i = 0; i < nr; ++i) {
-            uint32_t* hi = sl.h_idx + sl.req_off[i];
+            uint32_t* hi = reinterpret_cast<uint32_t*>(sl.h_out) + sl.req_off[i];
             for (uint64_t j = 0; j < reqs[i]->q; ++j) hi[j] = rmq::kNoPos;
         }
         std::vector<Request*> failed(sl.rptr.begin(), sl.rptr.end());
@@ -492,14 +496,11 @@ int rmq_server_create(const rmq_server_config* cfg_in, rmq_server** out) {
     for (Slot& sl : s->slots) {
         if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming);
-        if (e == cudaSuccess) e = cudaMallocHost(&sl.h_q, mq * 2 * sizeof(uint32_t));
-        if (e == cudaSuccess) e = cudaMallocHost(&sl.h_idx, mq * sizeof(uint32_t));
-        if (e == cudaSuccess) e = cudaMallocHost(&sl.h_min, mq * sizeof(float));
-        if (e == cudaSuccess) e = cudaMallocHost(&sl.h_hdr, header_bytes(mr));
-        if (e == cudaSuccess) e = cudaMalloc(&sl.d_q, mq * 2 * sizeof(uint32_t));
-        if (e == cudaSuccess) e = cudaMalloc(&sl.d_idx, mq * sizeof(uint32_t));
-        if (e == cudaSuccess) e = cudaMalloc(&sl.d_min, mq * sizeof(float));
-        if (e == cudaSuccess) e = cudaMalloc(&sl.d_hdr, header_bytes(mr));
+        const size_t in_bytes = header_bytes(mr) + mq * 2 * sizeof(uint32_t);
+        if (e == cudaSuccess) e = cudaMallocHost(&sl.h_in, in_bytes);
+        if (e == cudaSuccess) e = cudaMallocHost(&sl.h_out, mq * 8);
+        if (e == cudaSuccess) e = cudaMalloc(&sl.d_in, in_bytes);
+        if (e == cudaSuccess) e = cudaMalloc(&sl.d_out, mq * 8);
         if (e == cudaSuccess) e = cudaMalloc(&sl.d_owner, (mq / 32 + mr + 1) * sizeof(uint32_t));
     }
     if (e != cudaSuccess) {
@@ -638,14 +639,10 @@ void rmq_server_destroy(rmq_server* s) {
         if (sl.stream) cudaStreamSynchronize(sl.stream);
         if (sl.stream) cudaStreamDestroy(sl.stream);
         if (sl.done) cudaEventDestroy(sl.done);
-        cudaFreeHost(sl.h_q);
-        cudaFreeHost(sl.h_idx);
-        cudaFreeHost(sl.h_min);
-        cudaFreeHost(sl.h_hdr);
-        cudaFree(sl.d_q);
-        cudaFree(sl.d_idx);
-        cudaFree(sl.d_min);
-        cudaFree(sl.d_hdr);
+        cudaFreeHost(sl.h_in);
+        cudaFreeHost(sl.h_out);
+        cudaFree(sl.d_in);
+        cudaFree(sl.d_out);
         cudaFree(sl.d_owner);
     }
     if (s->build_stream) {
