@@ -10,9 +10,9 @@
 // results into the requests' host buffers, unpins arrays, wakes waiters),
 // marks admitted arrays ready when their build event completes, and whenever
 // a slot is free packs the pending requests whose arrays are ready (FIFO, up
-// to max_batch_queries) into it and launches: one H2D of descriptors + queries,
-// owner fill, one query kernel (the batched per-warp kernel, one descriptor
-// per request), one D2H of the results, event.  Requests arriving while batches run are
+// to max_batch_queries) into it and launches: one H2D of descriptors, work
+// units and queries, one query kernel (the batched per-warp kernel, one
+// descriptor per request), one D2H of the results, event.  Requests arriving while batches run are
 // admitted into the next free slot, so up to S batches overlap on the device
 // with builds of newly admitted arrays on their own stream.
 //
@@ -113,24 +113,26 @@ struct Slot {
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
     // One upload and one download per batch: in = descs | q_off | unit_off |
-    // queries (sized by the batch); out = argmin[nq] | min[nq].
+    // owner of each 32-query unit | queries (sized by the batch);
+    // out = argmin[nq] | min[nq].
     uint8_t* h_in = nullptr;   // pinned
     uint8_t* h_out = nullptr;  // pinned
     uint8_t* d_in = nullptr;
     uint8_t* d_out = nullptr;
     uint64_t nq = 0;           // queries of the batch in flight
-    uint32_t* d_owner = nullptr;
     std::vector<uint64_t> reqs;
     std::vector<Request*> rptr;     // stable element pointers (taken under the lock)
     std::vector<uint64_t> req_off;  // query offset of each request in the batch
     bool busy = false;
 };
 
-// Bytes of a batch's header for nr requests, rounded to 16 (the queries follow).
+// Bytes of a batch's header for nr requests, rounded to 16 (the owner table
+// follows), and of its owner table for `units` work units (the queries follow).
 size_t header_bytes(uint32_t nr) {
     const size_t b = size_t(nr) * sizeof(rmq::ArrayDesc) + 2 * size_t(nr + 1) * sizeof(uint64_t);
     return (b + 15) & ~size_t(15);
 }
+size_t owner_bytes(uint64_t units) { return (units * sizeof(uint32_t) + 15) & ~size_t(15); }
 
 }  // namespace
 
@@ -315,14 +317,19 @@ bool launch_batch(rmq_server* s, Slot& sl, std::unique_lock<std::mutex>& lk) {
     rmq::ArrayDesc* hd = reinterpret_cast<rmq::ArrayDesc*>(sl.h_in);
     uint64_t* hq = reinterpret_cast<uint64_t*>(sl.h_in + size_t(nr) * sizeof(rmq::ArrayDesc));
     uint64_t* hu = hq + (nr + 1);
-    uint32_t* h_q = reinterpret_cast<uint32_t*>(sl.h_in + hdr);
     std::memcpy(hd, descs.data(), nr * sizeof(rmq::ArrayDesc));
     hq[0] = 0;
     hu[0] = 0;
     for (uint32_t i = 0; i < nr; ++i) {
-        std::memcpy(h_q + 2 * sl.req_off[i], reqs[i]->h_lr, reqs[i]->q * 2 * sizeof(uint32_t));
         hq[i + 1] = hq[i] + reqs[i]->q;
         hu[i + 1] = hu[i] + (reqs[i]->q + 31) / 32;
+    }
+    uint32_t* h_owner = reinterpret_cast<uint32_t*>(sl.h_in + hdr);
+    const size_t qat = hdr + owner_bytes(hu[nr]);
+    uint32_t* h_q = reinterpret_cast<uint32_t*>(sl.h_in + qat);
+    for (uint32_t i = 0; i < nr; ++i) {
+        for (uint64_t u = hu[i]; u < hu[i + 1]; ++u) h_owner[u] = i;
+        std::memcpy(h_q + 2 * sl.req_off[i], reqs[i]->h_lr, reqs[i]->q * 2 * sizeof(uint32_t));
     }
     const rmq::ArrayDesc* dd = reinterpret_cast<const rmq::ArrayDesc*>(sl.d_in);
     const uint64_t* dq = reinterpret_cast<const uint64_t*>(sl.d_in + size_t(nr) * sizeof(rmq::ArrayDesc));
@@ -330,20 +337,19 @@ bool launch_batch(rmq_server* s, Slot& sl, std::unique_lock<std::mutex>& lk) {
     sl.nq = nq;
     uint32_t* d_idx = reinterpret_cast<uint32_t*>(sl.d_out);
     float* d_min = reinterpret_cast<float*>(sl.d_out + nq * sizeof(uint32_t));
-    cudaError_t e = cudaMemcpyAsync(sl.d_in, sl.h_in, hdr + nq * 2 * sizeof(uint32_t), cudaMemcpyHostToDevice,
+    cudaError_t e = cudaMemcpyAsync(sl.d_in, sl.h_in, qat + nq * 2 * sizeof(uint32_t), cudaMemcpyHostToDevice,
                                     sl.stream);
-    if (e == cudaSuccess) e = rmq::launch_fill_owner(du, nr, sl.d_owner, sl.stream);
     if (e == cudaSuccess) {
         rmq::BatchQueryArgs a;
         a.values = reinterpret_cast<const float*>(s->arena);
         a.descs = dd;
-        a.owner = sl.d_owner;
+        a.owner = reinterpret_cast<const uint32_t*>(sl.d_in + hdr);
         a.unit_off = du;
         a.q_off = dq;
         a.total_units = hu[nr];
         a.lvl_val = reinterpret_cast<const float*>(s->arena);
         a.lvl_idx = reinterpret_cast<const uint32_t*>(s->arena);
-        a.qs = reinterpret_cast<const uint2*>(sl.d_in + hdr);
+        a.qs = reinterpret_cast<const uint2*>(sl.d_in + qat);
         a.out_min = d_min;
         a.out_idx = d_idx;
         a.threads = s->cfg.query_threads;
@@ -372,8 +378,8 @@ bool launch_batch(rmq_server* s, Slot& sl, std::unique_lock<std::mutex>& lk) {
 void dispatcher_main(rmq_server* s) {
     cudaSetDevice(s->device);
 #if defined(__linux__)
-    // The dispatcher polls in-flight batches every 10 us; with Linux's default
-    // 50 us timer slack each of those waits would last ~60 us, and that delay
+    // The dispatcher polls in-flight batches every 4 us; with Linux's default
+    // 50 us timer slack each of those waits would last ~55 us, and that delay
     // lands on every request's latency.
     prctl(PR_SET_TIMERSLACK, 1UL, 0UL, 0UL, 0UL);
 #endif
@@ -425,7 +431,7 @@ void dispatcher_main(rmq_server* s) {
             }
             if (s->pending.empty()) break;
         }
-        if (!progressed) s->cv_work.wait_for(lk, std::chrono::microseconds(any_busy || !s->admitting.empty() ? 10 : 200));
+        if (!progressed) s->cv_work.wait_for(lk, std::chrono::microseconds(any_busy || !s->admitting.empty() ? 4 : 200));
     }
 }
 
@@ -496,12 +502,11 @@ int rmq_server_create(const rmq_server_config* cfg_in, rmq_server** out) {
     for (Slot& sl : s->slots) {
         if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming);
-        const size_t in_bytes = header_bytes(mr) + mq * 2 * sizeof(uint32_t);
+        const size_t in_bytes = header_bytes(mr) + owner_bytes(mq / 32 + mr) + mq * 2 * sizeof(uint32_t);
         if (e == cudaSuccess) e = cudaMallocHost(&sl.h_in, in_bytes);
         if (e == cudaSuccess) e = cudaMallocHost(&sl.h_out, mq * 8);
         if (e == cudaSuccess) e = cudaMalloc(&sl.d_in, in_bytes);
         if (e == cudaSuccess) e = cudaMalloc(&sl.d_out, mq * 8);
-        if (e == cudaSuccess) e = cudaMalloc(&sl.d_owner, (mq / 32 + mr + 1) * sizeof(uint32_t));
     }
     if (e != cudaSuccess) {
         cudaGetLastError();
@@ -643,7 +648,6 @@ void rmq_server_destroy(rmq_server* s) {
         cudaFreeHost(sl.h_out);
         cudaFree(sl.d_in);
         cudaFree(sl.d_out);
-        cudaFree(sl.d_owner);
     }
     if (s->build_stream) {
         cudaStreamSynchronize(s->build_stream);
