@@ -17,7 +17,13 @@ namespace rmq {
 // first), right pieces in descending order ("<=" lets the more-left sector
 // win), and a left/final winner beats a right winner on equal values.
 // Phase 2 re-reads only the winning sector, takes its first entry equal to the
-// minimum and, for a coarse level, that entry's stored level-0 index.
+// minimum and, for a coarse level, that entry's stored level-0 index (for
+// 32-bit handles the sector's eight indices come with the values).
+//
+// The thread's dependent chain of loads (one round trip per level) bounds the
+// kernel, so every round trip counts: the two boundary sectors of a level are
+// loaded together, forward scans take two sectors per round trip, and the
+// small top levels are read through L1 (kL1LevelEntries).
 // ---------------------------------------------------------------------------
 
 // L2 eviction priorities (tuning knobs; 0 selects the default shown).
