@@ -56,17 +56,18 @@ namespace {
 // Variant defaults.  VL: the paper's chosen configuration (rf = 8, t = 32,
 // scripts/static_data.py:251-253).  CL: the paper chose 16 lanes x 2 entries
 // (rf = 32, t = 64, scripts/get_and_filter_data.py:11); for this CL kernel
-// (lanes share whole 32-byte sectors) the best measured on GB300 is rf = 16
-// with 4 lanes per tile, t = 64.
-constexpr int kClRfLog = 4;
+// (lanes share whole 32-byte sectors, every lane walks each query's descent)
+// the best measured on GB300 is the smallest tile, 2 lanes, with rf = 8 and
+// t = 64 (n = q = 2^26: 16.1 G queries/s with argmin, against 10.7 at
+// rf = 16 with 4 lanes and 9.4 at rf = 8 with 4 lanes).
+constexpr int kClRfLog = 3;
 constexpr uint64_t kClT = 64;
-constexpr int kClLanes = 4;
+constexpr int kClLanes = 2;
 constexpr int kVlRfLog = 3;
 constexpr uint64_t kVlT = 32;
 // AUTO resolves to VL with rf = 8: measured on GB300 it is the fastest
-// work distribution at every batch size and array size tried (the
-// level-parallel CL kernel replicates the descent's index arithmetic on every
-// lane of the tile, which costs more than the memory round trips it saves).
+// work distribution at every batch size and array size tried (CL tiles
+// repeat each query's descent arithmetic on every lane of the tile).
 
 // Largest n of 32-bit handles: queries are uint32 pairs and the descent rounds
 // r up by at most rf - 1 without overflowing 32 bits.  64-bit handles take up
@@ -107,7 +108,7 @@ int resolve_config(uint64_t n, const rmq_config* cfg_in, int* variant, int* rf_l
     if (v == RMQ_VARIANT_CL && tt < 2 * rf) return RMQ_ERR_ARG;
     if (v == RMQ_VARIANT_VL && tt < rf) return RMQ_ERR_ARG;
     int g = cfg.lanes != 0 ? cfg.lanes : kClLanes;
-    if (g != 4 && g != 8 && g != 16 && g != 32) return RMQ_ERR_ARG;
+    if (g != 2 && g != 4 && g != 8 && g != 16 && g != 32) return RMQ_ERR_ARG;
     (void)n;
     *variant = v;
     *rf_log = r;

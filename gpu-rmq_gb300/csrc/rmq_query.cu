@@ -299,6 +299,7 @@ static cudaError_t launch_query_r(const QueryArgs& a, cudaStream_t s) {
                   : launch_with_window(query_cl_kernel<R, G, false>, grid, a, s, a.lv, a.qs, q32, a.out_min, \
                                        static_cast<uint32_t*>(nullptr), a.err)
     switch (a.lanes) {
+        case 2: RMQ_CL(2);
         case 4: RMQ_CL(4);
         case 8: RMQ_CL(8);
         case 16: RMQ_CL(16);

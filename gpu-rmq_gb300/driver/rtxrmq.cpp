@@ -113,7 +113,7 @@ void print_help() {
                  "   --data-dir <dir>          directory of that cache (default: .)\n"
                  "   --variant cl|vl|auto      work distribution of alg 22/122 (default: auto)\n"
                  "   --rf_log <3..5>           log2 of the reduction factor (default: variant's)\n"
-                 "   --lanes <4|8|16|32>       CL lanes per query\n"
+                 "   --lanes <2|4|8|16|32>     CL lanes per query\n"
                  "   --l2_persist              keep the coarse levels in an L2 persisting window\n"
                  "   --ties <frac>             set that fraction of entries to the global minimum\n");
 }

@@ -48,7 +48,7 @@ typedef enum {
 
 typedef enum {
     RMQ_VARIANT_AUTO = 0,  /* the measured best: VL with rf = 8                                          */
-    RMQ_VARIANT_CL = 1,    /* lane tile per query, lanes split the pieces by level (reference alg 16 family) */
+    RMQ_VARIANT_CL = 1,    /* tile of lanes answering its queries one after another (reference alg 16 family) */
     RMQ_VARIANT_VL = 2     /* one thread per query, 256-bit loads (reference alg 20 family)              */
 } rmq_variant;
 
@@ -56,7 +56,7 @@ typedef struct {
     int32_t  variant;         /* rmq_variant                                                    */
     uint64_t scan_threshold;  /* t: build levels while a level holds more than t entries (0 = variant default) */
     int32_t  rf_log;          /* log2 of the per-level reduction factor, 3..5 (0 = variant default)       */
-    int32_t  lanes;           /* CL: lanes cooperating on one query, 4/8/16/32 (0 = default)            */
+    int32_t  lanes;           /* CL: lanes cooperating on one query, 2/4/8/16/32 (0 = default)          */
     int32_t  with_index;      /* build the per-block argmin arrays (needed by rmq_query_idx)             */
     int32_t  l2_persist;      /* put the coarse levels in an L2 persisting access-policy window          */
     int32_t  validate;        /* count invalid queries on the device; query calls then synchronise       */

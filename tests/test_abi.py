@@ -62,7 +62,7 @@ def test_plan_layout_matches_oracle(variant, rf_log):
 
 def test_plan_layout_defaults_and_preconditions():
     cl = R.plan_layout(1 << 20, 0, 0, "cl")
-    assert cl.rf_log == 4 and cl.scan_threshold == 64 and cl.lanes == 4  # tuned CL: rf 16, 4 lanes, t 64
+    assert cl.rf_log == 3 and cl.scan_threshold == 64 and cl.lanes == 2  # tuned CL: rf 8, 2 lanes, t 64
     vl = R.plan_layout(1 << 20, 0, 0, "vl")
     assert vl.rf_log == 3 and vl.scan_threshold == 32  # paper's VL: rf 8, t 32
     # the reference's preconditions: t >= 2 rf (CL, src/xxx.h:211), t >= rf (VL, src/xxx.h:938)
