@@ -389,14 +389,14 @@ def run_ours(args, ws, rank, local):
     alg_bytes = algorithmic_bytes(qs, args.n, True, True)
     kernel_ms = statistics.mean(per_launch)
     achieved = alg_bytes / (kernel_ms / 1e3) / 1e9
-    kname = "vl" if info.variant == 2 else "cl"
-    tpq = traffic_per_query(f"{kname}-rf{1 << info.rf_log}")
+    tag = f"vl-rf{1 << info.rf_log}" if info.variant == 2 else f"cl-rf{1 << info.rf_log}-g{info.lanes}"
+    tpq = traffic_per_query(tag)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved / peaks["hbm_gbs"],
                 "traffic": (tpq * q) if tpq is not None else None,
                 "peak_source": f"{peaks['source']} (MEASURED_PEAKS.json hbm_gbs, copy burst)",
                 "algorithmic_bytes_per_launch": alg_bytes,
-                "kernel": f"query_{kname}_kernel (argmin+min)",
+                "kernel": f"query_{'vl' if info.variant == 2 else 'cl'}_kernel (argmin+min), {tag}",
                 "kernel_ms_mean": kernel_ms}
 
     cpu = None
