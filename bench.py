@@ -809,6 +809,9 @@ def parse_args(argv=None):
 def main(argv=None):
     args = parse_args(argv)
     ws, rank, local = dist_env()
+    if args.gpus != ws and rank == 0:
+        print(f"bench.py: --gpus {args.gpus} but WORLD_SIZE={ws}; one process per GPU is started by "
+              f"torchrun, and the line reports the {ws} rank(s) that run", file=sys.stderr)
     if args.impl == "reference":
         run_reference(args, ws, rank)
         return
