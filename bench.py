@@ -486,10 +486,61 @@ def run_e2e(args, h, qs, dev, ws, out_idx, out_min) -> dict:
     torch.cuda.synchronize()
     dt = max_over_ranks(time.perf_counter() - t0, ws, dev)
     same = bool(torch.equal(h_idx, out_idx.cpu()) and torch.equal(h_min.view(torch.int32), out_min.cpu().view(torch.int32)))
+    link = host_link_rates(h_q, h_idx, h_min, out_idx, out_min)
+    step_s = dt / args.steps
+    link["achieved_GBps"] = 16 * q / step_s / 1e9
+    link["frac_of_duplex"] = link["achieved_GBps"] / link["duplex_GBps"]
     return {"value": ws * q * args.steps / dt, "unit": UNIT, "h2d_bytes_per_step": 8 * q,
             "d2h_bytes_per_step": 8 * q,
             "api": "rmq_query_idx_host on page-locked host buffers (kernel reads / writes host memory)",
-            "kernel_launches_per_step": 1, "results_equal_device_call": same}
+            "kernel_launches_per_step": 1, "results_equal_device_call": same, "host_link": link}
+
+
+def host_link_rates(h_q, h_idx, h_min, d_idx, d_min, reps: int = 3) -> dict:
+    """The host link's own rates for the end-to-end step's bytes, by copy
+    engine: the queries host -> device, the two result arrays device ->
+    host, and both directions at once on two streams (the end-to-end step's
+    floor is its 16 bytes per query at the duplex rate).  Run after the
+    timed region; the result buffers receive the device results again."""
+    import torch
+    d_q = torch.empty_like(h_q, device=d_idx.device)
+    s_up, s_down = torch.cuda.Stream(), torch.cuda.Stream()
+    cur = torch.cuda.current_stream()
+
+    def up():
+        d_q.copy_(h_q, non_blocking=True)
+
+    def down():
+        h_idx.copy_(d_idx, non_blocking=True)
+        h_min.copy_(d_min, non_blocking=True)
+
+    def both():
+        s_up.wait_stream(cur)
+        s_down.wait_stream(cur)
+        with torch.cuda.stream(s_up):
+            up()
+        with torch.cuda.stream(s_down):
+            down()
+        cur.wait_stream(s_up)
+        cur.wait_stream(s_down)
+
+    def rate(fn, nbytes):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return nbytes / (e0.elapsed_time(e1) / reps / 1e3) / 1e9
+
+    nq = h_q.numel() * 4
+    nr = h_idx.numel() * 4 + h_min.numel() * 4
+    out = {"h2d_GBps": rate(up, nq), "d2h_GBps": rate(down, nr), "duplex_GBps": rate(both, nq + nr),
+           "what": "copy-engine rates of the same buffers (page-locked host <-> device)"}
+    del d_q
+    return out
 
 
 def run_batched(args, ws, rank, local):

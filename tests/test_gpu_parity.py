@@ -268,3 +268,43 @@ def test_full_size_large_mixed_ties(cuda):
     R.plant_min_ties(a, 0.01, 7)
     qs = R.gen_queries(q, -8, n, 7)
     _full_check(cuda, a, qs, 7, [("vl", 3, 0), ("cl", 5, 8)], [1 << 10])
+
+
+@pytest.mark.parametrize("n", [1025 * 8192, 1025 * 8192 + 5, 3 * (1 << 22) + 13, (1 << 24) + 8191])
+def test_streamed_build_sizes(cuda, n):
+    """Arrays of more than 1024 tiles of 8192 entries, whose level 0 streams
+    through shared memory by bulk copy (whole tiles) plus a global-load pass
+    for a partial last tile: every tile's block minima, heavy ties and signed
+    zeros, with queries spanning each tile, crossing each tile boundary and of
+    random lengths, against the GPU brute-force checker, for every reduction
+    factor and both variants at their smallest t (every level is read)."""
+    import torch
+    rng = np.random.default_rng(n)
+    a = rng.integers(-50, 50, n).astype(np.float32)
+    a[rng.random(n) < 0.02] = -0.0
+    a[rng.random(n) < 0.01] = 0.0
+    tiles = (n + 8191) // 8192
+    starts = np.arange(tiles, dtype=np.int64) * 8192
+    whole = np.stack([starts, np.minimum(starts + 8191, n - 1)], 1)
+    cross = np.stack([np.maximum(starts[1:] - 37, 0), np.minimum(starts[1:] + 100, n - 1)], 1)
+    l = rng.integers(0, n, 1 << 18)
+    ln = np.exp(rng.uniform(0, np.log(1 << 20), l.size)).astype(np.int64)
+    rnd = np.stack([l, np.minimum(l + ln, n - 1)], 1)
+    qs = np.concatenate([whole, cross, rnd]).astype(np.uint32)
+    dv = torch.from_numpy(a).to(cuda)
+    dq = torch.from_numpy(qs.view(np.int32)).to(cuda)
+    bm, bi = R.bruteforce(dv, dq)
+    for v, r, g in [("vl", 3, 0), ("vl", 4, 0), ("vl", 5, 0), ("cl", 3, 2), ("cl", 5, 8)]:
+        with R.Hierarchy(dv, variant=v, t=_t_for(v, r, 1), rf_log=r, lanes=g) as h:
+            i, m = h.query_idx(dq, with_min=True)
+            m1 = h.query(dq)
+        torch.cuda.synchronize()
+        assert torch.equal(m.view(torch.int32), bm.view(torch.int32)), f"{v} rf{1 << r} min"
+        assert torch.equal(m1.view(torch.int32), bm.view(torch.int32)), f"{v} rf{1 << r} min-only"
+        assert torch.equal(i, bi), f"{v} rf{1 << r} argmin"
+    # the same array under a 64-bit handle (64-bit positions in every level)
+    with R.Hierarchy(dv, variant="vl", t=8, rf_log=3, index_bits=64) as h:
+        i64, m64 = h.query_idx64(torch.from_numpy(qs.astype(np.int64)).to(cuda), with_min=True)
+    torch.cuda.synchronize()
+    assert torch.equal(m64.view(torch.int32), bm.view(torch.int32)), "64-bit min"
+    assert torch.equal(i64, bi.to(torch.int64)), "64-bit argmin"
