@@ -255,6 +255,14 @@ __device__ __forceinline__ float vl_descend(const LevelsT<I>& lv, I& l, I& r, ui
     return m;
 }
 
+// Unsigned key ordered like the float's value (NaN outside the contract):
+// negative values map below positive ones with their order reversed, and
+// -0.0 maps to the key of +0.0, as the two compare equal.
+__device__ __forceinline__ uint32_t min_key(float x) {
+    const uint32_t u = x == 0.0f ? 0u : __float_as_uint(x);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
 // Whole-warp scan of the final piece [lo, hi) of level k owned by lane
 // `owner`: lane j reads sectors j, j + 32, ... of the piece (1 KiB contiguous
 // per warp load), keeps its first sector holding its minimum, and the warp
@@ -278,13 +286,27 @@ __device__ __forceinline__ void warp_scan_final(const LevelsT<I>& lv, uint32_t k
             bs = s;
         }
     }
+    if constexpr (sizeof(I) == 4) {
+        // Two warp reductions (redux.sync): the smallest value, as an
+        // order-preserving key with both zeros on one key (they compare
+        // equal), then the lowest sector among lanes holding it; the winning
+        // lane supplies the value's own bits.  A lane that scanned nothing
+        // has sector kNone, the largest key.
+        const uint32_t vk = min_key(best);
+        const uint32_t mk = __reduce_min_sync(0xffffffffu, vk);
+        const uint32_t ws = __reduce_min_sync(0xffffffffu, vk == mk ? uint32_t(bs) : uint32_t(kNone));
+        const uint32_t wl = uint32_t(__ffs(__ballot_sync(0xffffffffu, vk == mk && uint32_t(bs) == ws)) - 1);
+        best = __shfl_sync(0xffffffffu, best, wl);
+        bs = I(ws);
+    } else {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        const float ov = __shfl_xor_sync(0xffffffffu, best, o);
-        const I os = __shfl_xor_sync(0xffffffffu, bs, o);
-        if (os != kNone && (bs == kNone || ov < best || (ov == best && os < bs))) {
-            best = ov;
-            bs = os;
+        for (int o = 16; o > 0; o >>= 1) {
+            const float ov = __shfl_xor_sync(0xffffffffu, best, o);
+            const I os = __shfl_xor_sync(0xffffffffu, bs, o);
+            if (os != kNone && (bs == kNone || ov < best || (ov == best && os < bs))) {
+                best = ov;
+                bs = os;
+            }
         }
     }
     if (lane == owner) {
