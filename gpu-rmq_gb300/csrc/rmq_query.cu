@@ -249,11 +249,11 @@ bruteforce_kernel(const float* __restrict__ a, uint32_t n, const uint2* __restri
 // ---------------------------------------------------------------------------
 
 template <typename K, typename... Args>
-static cudaError_t launch_with_window(K kernel, uint32_t grid, const QueryArgs& a, cudaStream_t s,
-                                      Args... args) {
+static cudaError_t launch_with_window_b(K kernel, uint32_t grid, uint32_t block, const QueryArgs& a,
+                                        cudaStream_t s, Args... args) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(256);
+    cfg.blockDim = dim3(block);
     cfg.dynamicSmemBytes = 0;
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
@@ -273,6 +273,11 @@ static cudaError_t launch_with_window(K kernel, uint32_t grid, const QueryArgs& 
     return cudaLaunchKernelEx(&cfg, kernel, args...);
 }
 
+template <typename K, typename... Args>
+static cudaError_t launch_with_window(K kernel, uint32_t grid, const QueryArgs& a, cudaStream_t s, Args... args) {
+    return launch_with_window_b(kernel, grid, 256u, a, s, args...);
+}
+
 template <int R>
 static cudaError_t launch_query_r(const QueryArgs& a, cudaStream_t s) {
     const bool argmin = a.out_idx != nullptr || a.out_idx64 != nullptr;
@@ -287,10 +292,17 @@ static cudaError_t launch_query_r(const QueryArgs& a, cudaStream_t s) {
                                            a.out_min, static_cast<uint64_t*>(nullptr), a.err);
     }
     if (a.variant == 2) {
-        return argmin ? launch_with_window(query_vl_kernel<R, true, uint32_t>, grid, a, s, a.lv, a.qs, a.q,
-                                           a.out_min, a.out_idx, a.err)
-                      : launch_with_window(query_vl_kernel<R, false, uint32_t>, grid, a, s, a.lv, a.qs, a.q,
-                                           a.out_min, static_cast<uint32_t*>(nullptr), a.err);
+        // 128-thread blocks: a block keeps its register slots until its
+        // deepest query ends, so smaller blocks give finished warps' slots
+        // back sooner (n = q = 2^26, vs 256: lognormal +0.5 %, three-way
+        // mixture +1.7 %, uniform lengths -0.5 %; 64 threads: +0.6 / +2.3 /
+        // -1 %).
+        constexpr uint32_t vb = 128u;
+        const uint32_t g2 = uint32_t((a.q + vb - 1u) / vb);
+        return argmin ? launch_with_window_b(query_vl_kernel<R, true, uint32_t>, g2, vb, a, s, a.lv, a.qs, a.q,
+                                             a.out_min, a.out_idx, a.err)
+                      : launch_with_window_b(query_vl_kernel<R, false, uint32_t>, g2, vb, a, s, a.lv, a.qs, a.q,
+                                             a.out_min, static_cast<uint32_t*>(nullptr), a.err);
     }
     const uint32_t q32 = uint32_t(a.q);
 #define RMQ_CL(G)                                                                                            \
