@@ -249,8 +249,8 @@ bruteforce_kernel(const float* __restrict__ a, uint32_t n, const uint2* __restri
 // ---------------------------------------------------------------------------
 
 template <typename K, typename... Args>
-static cudaError_t launch_with_window_b(K kernel, uint32_t grid, uint32_t block, const QueryArgs& a,
-                                        cudaStream_t s, Args... args) {
+static cudaError_t launch_with_window(K kernel, uint32_t grid, uint32_t block, const QueryArgs& a,
+                                      cudaStream_t s, Args... args) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
     cfg.blockDim = dim3(block);
@@ -273,43 +273,41 @@ static cudaError_t launch_with_window_b(K kernel, uint32_t grid, uint32_t block,
     return cudaLaunchKernelEx(&cfg, kernel, args...);
 }
 
-template <typename K, typename... Args>
-static cudaError_t launch_with_window(K kernel, uint32_t grid, const QueryArgs& a, cudaStream_t s, Args... args) {
-    return launch_with_window_b(kernel, grid, 256u, a, s, args...);
-}
+// Query kernels run in 128-thread blocks.  A block keeps its register slots
+// until its last query ends, so smaller blocks give finished warps' slots
+// back sooner; at the same registers per thread the SM holds as many warps
+// (VL 32-bit: 12 blocks of 128 = 6 of 256).  n = q = 2^26, lognormal
+// lengths, vs 256-thread blocks: VL +0.5 % (three-way mixture +1.7 %,
+// uniform lengths -0.5 %), VL with 64-bit positions +6.3 % (55 registers:
+// 9 blocks of 128 hold 36 warps, 4 of 256 held 32), CL (rf 8, 2 lanes)
+// +2.1 %.  64-thread blocks: within 1 % of these, uniform lengths -1 %.
+constexpr uint32_t kQueryBlock = 128;
 
 template <int R>
 static cudaError_t launch_query_r(const QueryArgs& a, cudaStream_t s) {
     const bool argmin = a.out_idx != nullptr || a.out_idx64 != nullptr;
-    const uint32_t grid = uint32_t((a.q + 255u) / 256u);
+    const uint32_t grid = uint32_t((a.q + kQueryBlock - 1u) / kQueryBlock);
     if (a.wide) {
         // 64-bit positions: the VL kernel only.
         if (a.variant != 2) return cudaErrorNotSupported;
         const ulonglong2* qs = reinterpret_cast<const ulonglong2*>(a.qs64);
-        return argmin ? launch_with_window(query_vl_kernel<R, true, uint64_t>, grid, a, s, a.lv64, qs, a.q,
-                                           a.out_min, a.out_idx64, a.err)
-                      : launch_with_window(query_vl_kernel<R, false, uint64_t>, grid, a, s, a.lv64, qs, a.q,
-                                           a.out_min, static_cast<uint64_t*>(nullptr), a.err);
+        return argmin ? launch_with_window(query_vl_kernel<R, true, uint64_t>, grid, kQueryBlock, a, s, a.lv64,
+                                             qs, a.q, a.out_min, a.out_idx64, a.err)
+                      : launch_with_window(query_vl_kernel<R, false, uint64_t>, grid, kQueryBlock, a, s, a.lv64,
+                                             qs, a.q, a.out_min, static_cast<uint64_t*>(nullptr), a.err);
     }
     if (a.variant == 2) {
-        // 128-thread blocks: a block keeps its register slots until its
-        // deepest query ends, so smaller blocks give finished warps' slots
-        // back sooner (n = q = 2^26, vs 256: lognormal +0.5 %, three-way
-        // mixture +1.7 %, uniform lengths -0.5 %; 64 threads: +0.6 / +2.3 /
-        // -1 %).
-        constexpr uint32_t vb = 128u;
-        const uint32_t g2 = uint32_t((a.q + vb - 1u) / vb);
-        return argmin ? launch_with_window_b(query_vl_kernel<R, true, uint32_t>, g2, vb, a, s, a.lv, a.qs, a.q,
-                                             a.out_min, a.out_idx, a.err)
-                      : launch_with_window_b(query_vl_kernel<R, false, uint32_t>, g2, vb, a, s, a.lv, a.qs, a.q,
-                                             a.out_min, static_cast<uint32_t*>(nullptr), a.err);
+        return argmin ? launch_with_window(query_vl_kernel<R, true, uint32_t>, grid, kQueryBlock, a, s, a.lv,
+                                             a.qs, a.q, a.out_min, a.out_idx, a.err)
+                      : launch_with_window(query_vl_kernel<R, false, uint32_t>, grid, kQueryBlock, a, s, a.lv,
+                                             a.qs, a.q, a.out_min, static_cast<uint32_t*>(nullptr), a.err);
     }
     const uint32_t q32 = uint32_t(a.q);
-#define RMQ_CL(G)                                                                                            \
-    return argmin ? launch_with_window(query_cl_kernel<R, G, true>, grid, a, s, a.lv, a.qs, q32, a.out_min,  \
-                                       a.out_idx, a.err)                                                     \
-                  : launch_with_window(query_cl_kernel<R, G, false>, grid, a, s, a.lv, a.qs, q32, a.out_min, \
-                                       static_cast<uint32_t*>(nullptr), a.err)
+#define RMQ_CL(G)                                                                                               \
+    return argmin ? launch_with_window(query_cl_kernel<R, G, true>, grid, kQueryBlock, a, s, a.lv, a.qs, q32,  \
+                                         a.out_min, a.out_idx, a.err)                                            \
+                  : launch_with_window(query_cl_kernel<R, G, false>, grid, kQueryBlock, a, s, a.lv, a.qs, q32, \
+                                         a.out_min, static_cast<uint32_t*>(nullptr), a.err)
     switch (a.lanes) {
         case 2: RMQ_CL(2);
         case 4: RMQ_CL(4);
