@@ -735,13 +735,14 @@ def run_serve(args, ws, rank, local):
     wrng = np.random.default_rng(args.seed + 7919)
     wsizes = [int(np.exp(wrng.uniform(np.log(2.0 ** 12), np.log(2.0 ** 20)))) for _ in range(32)]
     wev, wlr, _ = serve_trace(wrng, wsizes, 0.2, 20000.0, 0.05, args.seed + 7919)
-    with R.Server(hbm_budget_bytes=1 << 30, slots=args.serve_slots, t=64) as wsrv:
+    with R.Server(hbm_budget_bytes=1 << 30, slots=args.serve_slots, t=64,
+                  query_threads=args.serve_threads) as wsrv:
         for a, n in enumerate(wsizes):
             wsrv.register_generated(n, args.seed + 7919 + a)
         wq = int(wev["q"][wev["kind"] == 0].sum())
         wsrv.replay(wev, wlr, np.empty(wq, np.uint32), np.empty(wq, np.float32))
 
-    srv = R.Server(hbm_budget_bytes=64 << 30, slots=args.serve_slots, t=64)
+    srv = R.Server(hbm_budget_bytes=64 << 30, slots=args.serve_slots, t=64, query_threads=args.serve_threads)
     for a, n in enumerate(sizes):
         srv.register_generated(n, seed_of(a))
     warm = np.zeros((1, 2), dtype=np.uint32)
@@ -809,7 +810,8 @@ def run_serve(args, ws, rank, local):
                                "1..2^16 queries per request (log-uniform), lognormal(2^13, 1) lengths, "
                                "5 % registrations, 64 GiB budget, LRU eviction",
                    "seconds": args.serve_seconds, "events": int(ev.size), "requests": int(req.sum()),
-                   "queries": Q, "slots": args.serve_slots, "seed": args.seed},
+                   "queries": Q, "slots": args.serve_slots, "seed": args.seed,
+                   "query_threads": args.serve_threads or "library default"},
         "latency_us": {"p50": float(np.percentile(lat_req, 50)), "p99": float(np.percentile(lat_req, 99)),
                        "mean": float(lat_req.mean()), "max": float(lat_req.max())},
         "offered_queries_per_s": Q / float(ev["t_arrival_s"][-1]),
@@ -836,6 +838,8 @@ def parse_args(argv=None):
                          "serve = the request-serving loop")
     ap.add_argument("--serve-seconds", dest="serve_seconds", type=float, default=2.0)
     ap.add_argument("--serve-slots", dest="serve_slots", type=int, default=4)
+    ap.add_argument("--serve-threads", dest="serve_threads", type=int, default=0,
+                    help="CTA size of the served query kernel (0 = library default)")
     ap.add_argument("--batch-arrays", dest="batch_arrays", type=int, default=4096)
     ap.add_argument("--n", type=int, default=1 << 26)
     ap.add_argument("--q", type=int, default=1 << 26)

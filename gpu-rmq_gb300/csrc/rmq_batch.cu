@@ -175,7 +175,7 @@ struct rmq_batch {
     uint32_t num_arrays = 0;
     std::vector<uint64_t> val_off, sizes;
     uint64_t t = 64;
-    uint32_t qblock = 256;  // threads per CTA of the query kernel
+    uint32_t qblock = 128;  // threads per CTA of the query kernel (untuned default)
     int with_index = 1;
     int device = 0;
     // levels
@@ -210,7 +210,7 @@ namespace {
 
 constexpr uint64_t kBatchDefaultT = 64;
 constexpr uint64_t kTuneT[] = {16, 32, 64, 256, 1024};
-constexpr uint32_t kTuneBlock[] = {128, 256, 512};  // threads per CTA of the query kernel
+constexpr uint32_t kTuneBlock[] = {64, 128, 256, 512};  // threads per CTA of the query kernel
 
 int status_of(cudaError_t e) {
     if (e == cudaSuccess) return RMQ_OK;

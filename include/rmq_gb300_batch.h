@@ -66,7 +66,7 @@ int rmq_batch_run(rmq_batch* b, rmq_stream_t stream);
 
 /* Autotuner: times the query kernel on the registered queries for each
  * candidate scan threshold t in {16, 32, 64, 256, 1024} and CTA size in
- * {128, 256, 512} threads, keeps the fastest and rebuilds with it.
+ * {64, 128, 256, 512} threads, keeps the fastest and rebuilds with it.
  * Blocking.  The choice is reported in *info (may be NULL). */
 int rmq_batch_autotune(rmq_batch* b, rmq_stream_t stream, rmq_batch_info* info);
 

@@ -86,7 +86,7 @@ def test_batch_matches_oracle(cuda, seed):
             torch.cuda.synchronize()
             _check(out_min, out_idx, emin, eidx, f"graph run {rep}")
         info = b.autotune()
-        assert info.scan_threshold in (16, 32, 64, 256, 1024) and info.query_block in (128, 256, 512)
+        assert info.scan_threshold in (16, 32, 64, 256, 1024) and info.query_block in (64, 128, 256, 512)
         out_min.fill_(-1)
         out_idx.fill_(-1)
         b.run()
