@@ -15,6 +15,17 @@
 
 namespace rmq {
 
+// Programmatic dependent launch: the kernels after the fused one are launched
+// with programmatic stream serialization, so they are scheduled while the
+// previous kernel's last CTAs still run and wait here (griddepcontrol.wait
+// returns once the previous grid has completed and its writes are visible;
+// in a kernel launched without the attribute it returns at once).
+__device__ __forceinline__ void wait_previous_grid() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+// Lets the next kernel of the stream be scheduled (its CTAs then wait in
+// wait_previous_grid until this grid completes).
+__device__ __forceinline__ void allow_next_grid() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 // One output block per group of LPB = rf/8 lanes (P: position type).
 //   src, src_size : level k (level 0 = caller's array, not padded)
 //   src_idx       : level-0 indices of level k's entries (null for k = 0)
@@ -25,6 +36,8 @@ build_step_kernel(const float* __restrict__ src, const P* __restrict__ src_idx, 
                   float* __restrict__ dst, P* __restrict__ dst_idx, P dst_size) {
     constexpr uint32_t LPB = (1u << R) / 8u;
     constexpr P kNone = IdxTraits<P>::none;
+    wait_previous_grid();
+    allow_next_grid();
     const uint64_t gt = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     const P blk = P(gt / LPB);
     const uint32_t sub = uint32_t(gt % LPB);
@@ -100,13 +113,32 @@ __global__ void __launch_bounds__(kFusedThreads)
 build_fused_kernel(const float* __restrict__ a, P n, LevelOutT<P> out, uint32_t depth, TailPlan tp) {
     __shared__ float sv[kTileSectors];
     __shared__ P sp[kTileSectors];
+    allow_next_grid();
     fused_tile<R>(a, n, out, depth, blockIdx.x, sv, sp);
     if (tp.top > tp.depth) tail_upward<R>(out, tp, blockIdx.x);
 }
 
 template <int R, typename P>
 __global__ void __launch_bounds__(1024) build_tail_kernel(LevelOutT<P> out, uint32_t from, uint32_t last) {
+    wait_previous_grid();
     tail_levels<R>(out, from, last);
+}
+
+// Launch with programmatic stream serialization (see wait_previous_grid).
+template <typename... KArgs, typename... Args>
+static cudaError_t launch_dependent(void (*kernel)(KArgs...), uint32_t grid, uint32_t block, cudaStream_t s,
+                                    Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
 }
 
 template <int R>
@@ -195,14 +227,12 @@ static cudaError_t build_levels(const Layout& lay, const float* d_values, float*
         const P dst_size = out.size[k + 1];
         const uint64_t threads = uint64_t(dst_size) * LPB;
         const uint32_t grid = uint32_t((threads + 255) / 256);
-        build_step_kernel<R, P><<<grid, 256, 0, s>>>(out.val[k], out.idx[k], out.size[k], 1, out.val[k + 1],
-                                                    out.idx[k + 1], dst_size);
-        e = cudaGetLastError();
+        e = launch_dependent(build_step_kernel<R, P>, grid, 256, s, out.val[k], (const P*)out.idx[k], out.size[k],
+                             1, out.val[k + 1], out.idx[k + 1], dst_size);
         if (e != cudaSuccess) return e;
     }
     if (tail) {
-        build_tail_kernel<R, P><<<1, 1024, 0, s>>>(out, k, lay.num_levels - 1);
-        e = cudaGetLastError();
+        e = launch_dependent(build_tail_kernel<R, P>, 1, 1024, s, out, k, lay.num_levels - 1);
     }
     return e;
 }
