@@ -3,7 +3,7 @@
 // The structure is the reference's multi-level block-minimum hierarchy
 // (metadata struct src/constants.cuh:34-39, layout loop src/xxx.h:225-243):
 // level 0 is the caller's array; level k+1 holds, for every aligned chunk of
-// rf = 2^R entries of level k, the chunk minimum.  This build also stores,
+// rf = 2^R entries of level k, the chunk minimum.  The hierarchy here also stores,
 // next to every block minimum, the level-0 index of its first occurrence so
 // that argmin queries need one extra load instead of a second descent.
 #pragma once

@@ -72,7 +72,7 @@ extern "C" int rmq_query_idx_static(const float* d_values, uint64_t n, uint64_t 
     uint32_t* idx_buf = reinterpret_cast<uint32_t*>(val_buf + lay.total);
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
 
-    // Every level entry a query reads is rewritten by this build, so nothing
+    // Every level entry a query reads is rewritten by the build of this call, so nothing
     // in the scratch needs clearing between calls.
     cudaError_t e = rmq::launch_build(lay, d_values, val_buf, idx_buf, s);
     if (e == cudaSuccess && q > 0) {

@@ -10,7 +10,7 @@
 // --randTrivialCheck; src/main.cu:194-283).  Checks here are bit-exact
 // (the reference compares values with an absolute epsilon, src/tools.h:261).
 //
-// Algorithms of this build:
+// Algorithms of this driver:
 //     0  [CPU] BASE            brute-force scan, OpenMP   (src/cpu_methods.h:18)
 //   100  [CPU] BASE IDX        its argmin                 (src/cpu_methods.h:55)
 //     2  [GPU] BASE            brute-force scan           (src/cuda_methods.cuh:72)
@@ -132,7 +132,7 @@ bool parse(int argc, char** argv, Args& a) {
         return false;
     }
     if (a.n > 0xFFFFFF00ull) {
-        std::fprintf(stderr, "Error: n=%llu is above this build's limit (uint32 queries)\n",
+        std::fprintf(stderr, "Error: n=%llu is above this driver's limit (uint32 queries)\n",
                      (unsigned long long)a.n);
         return false;
     }
@@ -454,7 +454,7 @@ void write_csv(const Args& a, const Result& r, int check_code) {
         return;
     }
     // Column schema of create_XXX_header / create_header (src/tools.h:508-524),
-    // with this build's columns appended after checkResult.
+    // with this driver's columns appended after checkResult.
     if (!exists) {
         if (hier)
             std::fprintf(fp, "dev,alg,nt,reps,n,bs,nb,q,lr,GPU_BSIZE,CG_GROUP_SIZE,CG_MEM_ALIGNMENT,timestamp,"
@@ -505,12 +505,12 @@ int main(int argc, char** argv) {
     if (!parse(argc, argv, a)) return EXIT_FAILURE;
     if (a.alg == 16 || a.alg == 20 || a.alg == 17 || a.alg == 18 || a.alg == 19 || a.alg == 21 ||
         a.alg == 23 || a.alg == 24) {
-        std::fprintf(stderr, "Error: alg %d is one of the reference's own kernels; this build runs "
+        std::fprintf(stderr, "Error: alg %d is one of the reference's own kernels; this driver runs "
                              "alg 22 --variant cl (CL) or --variant vl (VL)\n", a.alg);
         return EXIT_FAILURE;
     }
     if (std::string(alg_name(a.alg)).empty()) {
-        std::fprintf(stderr, "Error: alg %d is not available in this build\n", a.alg);
+        std::fprintf(stderr, "Error: alg %d is not available in this driver\n", a.alg);
         print_help();
         return EXIT_FAILURE;
     }

@@ -43,7 +43,7 @@ typedef enum {
     RMQ_ERR_QUERY_RANGE = 4,  /* at least one query had l > r or r >= n (validate mode) */
     RMQ_ERR_TIMEOUT = 5,      /* a bounded device-side wait gave up */
     RMQ_ERR_NO_INDEX = 6,     /* argmin asked of a handle built with with_index = 0 */
-    RMQ_ERR_UNSUPPORTED = 7   /* size or configuration outside what this build supports */
+    RMQ_ERR_UNSUPPORTED = 7   /* size or configuration outside what this library supports */
 } rmq_status;
 
 typedef enum {

@@ -27,7 +27,7 @@ def test_help_and_bad_arguments():
     assert run(100, 10, -9, 0, "--seed", 1).returncode != 0  # unknown law
     r = run(100, 10, -1, 16)
     assert r.returncode != 0 and "variant cl" in r.stderr  # reference-only kernel ids
-    assert run(100, 10, -1, 5).returncode != 0  # not in this build
+    assert run(100, 10, -1, 5).returncode != 0  # not in this driver
 
 
 @pytest.mark.parametrize("alg", [0, 100])
