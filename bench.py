@@ -374,7 +374,7 @@ def run_ours(args, ws, rank, local):
     min_only_qps = q * args.steps / (min_ms / 1e3)
 
     # --- end to end: pinned host queries -> device -> host results -------------
-    e2e = run_e2e(args, h, qs, dev, ws, out_idx, out_min)
+    e2e = run_e2e(args, h, qs, dev, ws, out_idx, out_min, dq)
 
     # --- parity spot check of the timed outputs (not timed) ---------------------
     from oracle import oracle
@@ -459,7 +459,7 @@ def run_ours(args, ws, rank, local):
         dist.destroy_process_group()
 
 
-def run_e2e(args, h, qs, dev, ws, out_idx, out_min) -> dict:
+def run_e2e(args, h, qs, dev, ws, out_idx, out_min, d_q) -> dict:
     """Same metric through the C ABI with host buffers: every step is one
     rmq_query_idx_host call on page-locked host buffers (queries in, min +
     argmin out); with page-locked buffers the library's kernel reads the
@@ -490,10 +490,39 @@ def run_e2e(args, h, qs, dev, ws, out_idx, out_min) -> dict:
     step_s = dt / args.steps
     link["achieved_GBps"] = 16 * q / step_s / 1e9
     link["frac_of_duplex"] = link["achieved_GBps"] / link["duplex_GBps"]
+    link["kernel_ms_by_buffer_placement"] = placement_breakdown(h, q, d_q, out_idx, out_min, h_q, h_idx, h_min)
     return {"value": ws * q * args.steps / dt, "unit": UNIT, "h2d_bytes_per_step": 8 * q,
             "d2h_bytes_per_step": 8 * q,
             "api": "rmq_query_idx_host on page-locked host buffers (kernel reads / writes host memory)",
             "kernel_launches_per_step": 1, "results_equal_device_call": same, "host_link": link}
+
+
+def placement_breakdown(h, q, d_q, d_idx, d_min, h_q, h_idx, h_min, reps: int = 5) -> dict:
+    """The query kernel's time (CUDA events, ms per launch) with queries and
+    results each in device memory or in page-locked host memory (the kernel
+    reaching host memory over the link), through rmq_query_idx: where the
+    end-to-end step's time over the device-resident one goes.  Run after the
+    timed region; the result buffers receive the same results again."""
+    import torch
+    out = {}
+    for name, lq, oi, om in (("device queries, device results", d_q, d_idx, d_min),
+                             ("host queries, device results", h_q, d_idx, d_min),
+                             ("device queries, host results", d_q, h_idx, h_min),
+                             ("host queries, host results", h_q, h_idx, h_min)):
+        def launch():
+            st = h.query_idx_raw(int(lq.data_ptr()), q, int(oi.data_ptr()), int(om.data_ptr()))
+            if st != 0:
+                raise RuntimeError(f"rmq_query_idx failed: {st}")
+        launch()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            launch()
+        e1.record()
+        torch.cuda.synchronize()
+        out[name] = e0.elapsed_time(e1) / reps
+    return out
 
 
 def host_link_rates(h_q, h_idx, h_min, d_idx, d_min, reps: int = 3) -> dict:
