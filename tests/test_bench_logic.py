@@ -35,6 +35,39 @@ def test_level0_sectors_matches_brute_force():
         assert np.array_equal(got, want), n
 
 
+def _coarse_brute(l: int, r: int, n: int) -> int:
+    """Sectors of levels >= 1 read by the canonical descent (rf 32, t 64),
+    walking the levels one query at a time."""
+    rf, t = 32, 64
+    sizes = [n]
+    while len(sizes) < 20 and sizes[-1] > t:
+        sizes.append(-(-sizes[-1] // rf))
+    top = len(sizes) - 1
+    lo, e, k, total = l, r + 1, 0, 0
+    while k < top and e - lo > 2 * rf:
+        nl = -(-lo // rf) * rf
+        pr = e // rf * rf
+        if k > 0:
+            total += len({p // 8 for p in range(lo, nl)}) + len({p // 8 for p in range(pr, e)})
+        lo, e, k = nl // rf, pr // rf, k + 1
+    if k > 0:
+        total += len({p // 8 for p in range(lo, e)})
+    return total
+
+
+def test_coarse_sectors_matches_brute_force():
+    rng = np.random.default_rng(2)
+    for n in (1, 64, 65, 5000, 1 << 16, 1 << 22):
+        q = 400
+        length = np.minimum(rng.integers(1, n + 1, q), n)
+        length[: q // 4] = np.minimum(np.exp(rng.uniform(0, np.log(n + 1), q // 4)).astype(np.int64) + 1, n)
+        l = (rng.random(q) * (n - length + 1)).astype(np.int64)
+        qs = np.stack([l, l + length - 1], 1).astype(np.uint32)
+        got = bench.coarse_sectors(qs, n)
+        want = [_coarse_brute(int(a), int(b), n) for a, b in qs]
+        assert np.array_equal(got, want), n
+
+
 def test_algorithmic_bytes_counts_query_and_results():
     qs = np.array([[0, 0], [0, 63], [5, 200]], dtype=np.uint32)
     s = int(bench.level0_sectors(qs, 1000).sum())
