@@ -335,6 +335,29 @@ __device__ __forceinline__ float vl_phase1(const LevelsT<I>& lv, bool active, I 
         else is_long = true;
     }
     uint32_t pending = __ballot_sync(0xffffffffu, is_long);
+    if (pending != 0u && lv.size[lv.num_levels - 1] <= kL1LevelEntries) {
+        // Long pieces lie in the top level.  When it is read through L1, the
+        // scans are latency-bound: whole-warp scans take one round trip per
+        // 32 sectors of each long piece, one piece after another; lane-private
+        // scans one round trip per two sectors of the longest piece, all
+        // pieces at once.  The warp takes whichever needs fewer round trips
+        // (many long pieces: private; a few: whole-warp).  A larger top level
+        // is read from L2, where the whole-warp scans' contiguous 1 KiB loads
+        // use L2 better (lane-private scans of a 2^16-entry top level: -29 %).
+        // Both visit a piece's sectors in ascending order with the same fold,
+        // so the results are the same.
+        uint32_t sec = 0;
+        if (is_long) {
+            const uint64_t span = uint64_t(((r - 1u) >> 3) - (l >> 3)) + 1u;
+            sec = span < (1u << 26) ? uint32_t(span) : (1u << 26);
+        }
+        const uint32_t warp_trips = __reduce_add_sync(0xffffffffu, (sec + 31u) >> 5);
+        const uint32_t lane_trips = __reduce_max_sync(0xffffffffu, (sec + 1u) >> 1);
+        if (lane_trips < warp_trips) {
+            if (is_long) scan_fwd<ARGMIN>(lv, k, l, r, pol, m, tl);
+            pending = 0u;
+        }
+    }
     while (pending != 0u) {
         const uint32_t owner = uint32_t(__ffs(pending) - 1);
         const uint32_t ok = __shfl_sync(0xffffffffu, k, owner);
