@@ -293,7 +293,7 @@ def run_reference(args, ws, rank):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": workload_config(args),
+        "config": workload_config(args, "not applicable (host CPU run, a bounded sample of the queries per step)"),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{per_step} consecutive queries per step (random offset), "
                                    f"min + argmin brute-force scan on {threads} threads"},

@@ -111,3 +111,26 @@ def test_workload_names_follow_the_length_law():
 def test_traffic_figures_are_committed(tag):
     v = bench.traffic_per_query(tag)
     assert v is not None and 100.0 < v < 400.0
+
+
+def test_reference_arm_line_on_cpu():
+    """`bench.py --impl reference` runs the oracle's CPU scan on the host
+    only, and prints one JSON line with the contract's keys."""
+    import json
+    import subprocess
+    import sys
+    from pathlib import Path
+    root = Path(__file__).resolve().parents[1]
+    out = subprocess.run([sys.executable, str(root / "bench.py"), "--impl", "reference", "--steps", "2",
+                          "--warmup", "3", "--n", "65536", "--q", "4096", "--lr", "-1",
+                          "--ref-step-queries", "1024"],
+                         capture_output=True, text=True, timeout=300, cwd=root)
+    assert out.returncode == 0, out.stderr[-2000:]
+    line = json.loads(out.stdout.strip().splitlines()[-1])
+    for key in ("impl", "metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step",
+                "higher_is_better", "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert key in line, key
+    assert line["impl"] == "reference" and line["value"] > 0 and line["steps"] == 2
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
+    assert line["config"]["workload"].startswith("plain single array")
