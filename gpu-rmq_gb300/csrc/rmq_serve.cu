@@ -38,53 +38,13 @@
 
 #include "../../include/rmq_gb300_batch.h"
 #include "../../include/rmq_gb300_serve.h"
+#include "rmq_arena.h"
 #include "rmq_internal.h"
 
 namespace {
 
 using Clock = std::chrono::steady_clock;
-constexpr uint64_t kGranule = 256;
-
-uint64_t round_up(uint64_t x) { return (x + kGranule - 1) & ~(kGranule - 1); }
-
-class Arena {
-public:
-    void init(uint64_t size) {
-        free_.clear();
-        free_[0] = size;
-    }
-    bool alloc(uint64_t bytes, uint64_t* off) {
-        bytes = round_up(bytes);
-        for (auto it = free_.begin(); it != free_.end(); ++it) {
-            if (it->second < bytes) continue;
-            const uint64_t o = it->first, rest = it->second - bytes;
-            free_.erase(it);
-            if (rest) free_[o + bytes] = rest;
-            *off = o;
-            return true;
-        }
-        return false;
-    }
-    void release(uint64_t off, uint64_t bytes) {
-        bytes = round_up(bytes);
-        auto it = free_.emplace(off, bytes).first;
-        auto next = std::next(it);
-        if (next != free_.end() && off + bytes == next->first) {
-            it->second += next->second;
-            free_.erase(next);
-        }
-        if (it != free_.begin()) {
-            auto prev = std::prev(it);
-            if (prev->first + prev->second == it->first) {
-                prev->second += it->second;
-                free_.erase(it);
-            }
-        }
-    }
-
-private:
-    std::map<uint64_t, uint64_t> free_;
-};
+using rmq::Arena;
 
 struct ServedArray {
     uint64_t n = 0, seed = 0;
@@ -443,9 +403,9 @@ int register_array(rmq_server* s, uint64_t n, uint64_t seed, const float* host, 
     a.seed = seed;
     a.host = host;
     a.lay = rmq::plan_layout(n, s->cfg.scan_threshold, 3);
-    a.val_bytes = round_up(n * sizeof(float));
+    a.val_bytes = rmq::arena_round_up(n * sizeof(float));
     const uint64_t lvl_entries = a.lay.num_levels > 1 ? a.lay.total : 0;
-    a.lvl_bytes = round_up(lvl_entries * sizeof(float));
+    a.lvl_bytes = rmq::arena_round_up(lvl_entries * sizeof(float));
     a.bytes = a.val_bytes + 2 * a.lvl_bytes;
     if (a.bytes > s->cfg.hbm_budget_bytes) return RMQ_ERR_OOM;
     if (cudaEventCreateWithFlags(&a.built, cudaEventDisableTiming) != cudaSuccess) return RMQ_ERR_CUDA;
