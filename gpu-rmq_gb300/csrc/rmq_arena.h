@@ -61,4 +61,20 @@ private:
     std::map<uint64_t, uint64_t> free_;
 };
 
+// Eviction choice: the index of the least recently used array that may be
+// evicted (resident, built, no batch in flight, and not `except`), or
+// ~0 when none may.  Elements need `resident`, `ready`, `pins`, `last_use`.
+template <typename Arrays>
+uint64_t lru_victim(const Arrays& arrays, uint64_t except) {
+    uint64_t victim = ~uint64_t(0), oldest = ~uint64_t(0);
+    for (uint64_t i = 0; i < uint64_t(arrays.size()); ++i) {
+        const auto& c = arrays[i];
+        if (i != except && c.resident && c.ready && c.pins == 0 && c.last_use < oldest) {
+            oldest = c.last_use;
+            victim = i;
+        }
+    }
+    return victim;
+}
+
 }  // namespace rmq

@@ -151,14 +151,7 @@ bool admit(rmq_server* s, uint64_t id) {
     ServedArray& a = s->arrays[id];
     uint64_t off = 0;
     while (!s->alloc.alloc(a.bytes, &off)) {
-        uint64_t victim = ~uint64_t(0), oldest = ~uint64_t(0);
-        for (uint64_t i = 0; i < s->arrays.size(); ++i) {
-            const ServedArray& c = s->arrays[i];
-            if (i != id && c.resident && c.ready && c.pins == 0 && c.last_use < oldest) {
-                oldest = c.last_use;
-                victim = i;
-            }
-        }
+        const uint64_t victim = rmq::lru_victim(s->arrays, id);
         if (victim == ~uint64_t(0)) return false;
         evict(s, victim);
     }

@@ -2,7 +2,9 @@
 on the CPU: a seeded random sequence of allocations and releases against a
 byte-exact model.  Checks first fit (lowest offset that holds the request),
 256-byte granules, no overlap of live ranges, and that released ranges merge
-so the free list always covers exactly the bytes not in use."""
+so the free list always covers exactly the bytes not in use; and the
+eviction choice (least recently used among resident, built, unpinned
+arrays other than the one being admitted)."""
 from __future__ import annotations
 
 import shutil
@@ -92,3 +94,20 @@ def test_arena_against_model(harness, seed):
             assert pos == size
             for (o1, l1), (o2, _) in zip(ranges, ranges[1:]):
                 assert o1 + l1 < o2  # neighbours were merged
+
+
+def test_lru_victim_against_model(harness):
+    rng = np.random.default_rng(5)
+    cmds, expect = [], []
+    for _ in range(300):
+        n = int(rng.integers(0, 12))
+        rows = [(int(rng.random() < 0.7), int(rng.random() < 0.8), int(rng.random() < 0.2),
+                 int(rng.integers(0, 50))) for _ in range(n)]
+        except_ = int(rng.integers(0, max(1, n)))
+        cmds.append(f"v {except_} {n} " + " ".join(f"{a} {b} {c} {d}" for a, b, c, d in rows))
+        best, oldest = None, None
+        for i, (res, rdy, pins, last) in enumerate(rows):
+            if i != except_ and res and rdy and pins == 0 and (oldest is None or last < oldest):
+                best, oldest = i, last
+        expect.append("victim none" if best is None else f"victim {best}")
+    assert _run(harness, cmds) == expect
