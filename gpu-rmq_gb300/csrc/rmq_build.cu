@@ -9,7 +9,9 @@
 // (tail_upward: the tile completing a group computes the group's entry).  Every block
 // stores its first-occurring minimum and that entry's level-0 index, which
 // argmin queries use.  build_step_kernel (one level step, rf/8 lanes per
-// block) covers large intermediate levels of very large arrays.
+// block) covers large intermediate levels of very large arrays.  The kernels
+// after the fused one are chained by programmatic dependent launch, so each
+// is scheduled before its predecessor ends and no launch gap separates them.
 #include "rmq_internal.h"
 #include "rmq_buildk.cuh"
 

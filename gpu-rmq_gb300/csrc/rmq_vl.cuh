@@ -23,7 +23,9 @@ namespace rmq {
 // The thread's dependent chain of loads (one round trip per level) bounds the
 // kernel, so every round trip counts: the two boundary sectors of a level are
 // loaded together, forward scans take two sectors per round trip, and the
-// small top levels are read through L1 (kL1LevelEntries).
+// small top levels are read through L1 (kL1LevelEntries).  Final pieces
+// longer than kLongScan (top level only) are scanned by the whole warp one
+// after another or, when that takes more round trips, by their own lanes.
 // ---------------------------------------------------------------------------
 
 // L2 eviction priorities (tuning knobs; 0 selects the default shown).
