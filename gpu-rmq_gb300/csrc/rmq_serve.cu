@@ -26,6 +26,7 @@
 #include <condition_variable>
 #include <cstring>
 #include <deque>
+#include <limits>
 #include <map>
 #include <mutex>
 #include <new>
@@ -116,6 +117,7 @@ struct rmq_server {
     bool stop = false;
     uint64_t use_clock = 0;
     uint64_t not_done = 0;
+    uint32_t fail_batches = 0;  // injected launch failures still to come
     rmq_server_stats stats{};
 };
 
@@ -186,13 +188,24 @@ bool admit(rmq_server* s, uint64_t id) {
 }
 
 // Copies a finished slot's results out and completes its requests.  Called
-// without mu held (the slot and its requests belong to the dispatcher).
-void finish_slot(rmq_server* s, Slot& sl) {
-    std::vector<int> status(sl.reqs.size(), RMQ_OK);
+// without mu held (the slot and its requests belong to the dispatcher).  With
+// `failed` set (the batch's launch failed) every request of the slot gets
+// that status and all-ones argmin / NaN minima instead of results; the status
+// is set under mu together with `done`, so a waiter never sees one without
+// the other.
+void finish_slot(rmq_server* s, Slot& sl, int failed = RMQ_OK) {
+    std::vector<int> status(sl.reqs.size(), failed);
     const uint32_t* h_idx = reinterpret_cast<const uint32_t*>(sl.h_out);
     const float* h_min = reinterpret_cast<const float*>(sl.h_out + sl.nq * sizeof(uint32_t));
     for (size_t i = 0; i < sl.reqs.size(); ++i) {
         Request& r = *sl.rptr[i];
+        if (failed != RMQ_OK) {
+            for (uint64_t j = 0; j < r.q; ++j) {
+                if (r.h_idx != nullptr) r.h_idx[j] = rmq::kNoPos;
+                if (r.h_min != nullptr) r.h_min[j] = std::numeric_limits<float>::quiet_NaN();
+            }
+            continue;
+        }
         const uint64_t o = sl.req_off[i];
         if (r.h_idx != nullptr) std::memcpy(r.h_idx, h_idx + o, r.q * sizeof(uint32_t));
         if (r.h_min != nullptr) std::memcpy(r.h_min, h_min + o, r.q * sizeof(float));
@@ -263,6 +276,8 @@ bool launch_batch(rmq_server* s, Slot& sl, std::unique_lock<std::mutex>& lk) {
     std::vector<rmq::ArrayDesc> descs(nr);
     std::vector<const Request*> reqs(sl.rptr.begin(), sl.rptr.end());
     for (uint32_t i = 0; i < nr; ++i) descs[i] = describe(s->arrays[reqs[i]->array]);
+    const bool inject = s->fail_batches > 0;
+    if (inject) s->fail_batches--;
     lk.unlock();
 
     // Upload: descriptors | q_off[nr + 1] | unit_off[nr + 1] | queries.
@@ -290,8 +305,11 @@ bool launch_batch(rmq_server* s, Slot& sl, std::unique_lock<std::mutex>& lk) {
     sl.nq = nq;
     uint32_t* d_idx = reinterpret_cast<uint32_t*>(sl.d_out);
     float* d_min = reinterpret_cast<float*>(sl.d_out + nq * sizeof(uint32_t));
-    cudaError_t e = cudaMemcpyAsync(sl.d_in, sl.h_in, qat + nq * 2 * sizeof(uint32_t), cudaMemcpyHostToDevice,
-                                    sl.stream);
+    // An injected failure (rmq_server_fail_next_batches) stands in for a
+    // failing upload: nothing is issued and the batch takes the error path.
+    cudaError_t e = inject ? cudaErrorInvalidConfiguration
+                           : cudaMemcpyAsync(sl.d_in, sl.h_in, qat + nq * 2 * sizeof(uint32_t),
+                                             cudaMemcpyHostToDevice, sl.stream);
     if (e == cudaSuccess) {
         rmq::BatchQueryArgs a;
         a.values = reinterpret_cast<const float*>(s->arena);
@@ -311,17 +329,11 @@ bool launch_batch(rmq_server* s, Slot& sl, std::unique_lock<std::mutex>& lk) {
     if (e == cudaSuccess) e = cudaMemcpyAsync(sl.h_out, sl.d_out, nq * 8, cudaMemcpyDeviceToHost, sl.stream);
     if (e == cudaSuccess) e = cudaEventRecord(sl.done, sl.stream);
     if (e != cudaSuccess) {
-        // Launch failure: fail the batch's requests (results undefined).
+        // Launch failure: the batch's requests complete with RMQ_ERR_CUDA.
         cudaGetLastError();
         cudaStreamSynchronize(sl.stream);
-        for (uint32_t i = 0; i < nr; ++i) {
-            uint32_t* hi = reinterpret_cast<uint32_t*>(sl.h_out) + sl.req_off[i];
-            for (uint64_t j = 0; j < reqs[i]->q; ++j) hi[j] = rmq::kNoPos;
-        }
-        std::vector<Request*> failed(sl.rptr.begin(), sl.rptr.end());
-        finish_slot(s, sl);
+        finish_slot(s, sl, RMQ_ERR_CUDA);
         lk.lock();
-        for (Request* r : failed) r->status = RMQ_ERR_CUDA;
         return true;
     }
     lk.lock();
@@ -571,6 +583,31 @@ int rmq_server_replay(rmq_server* s, const rmq_trace_event* ev, uint64_t count, 
     }
     if (wall_s) *wall_s = first == Clock::time_point::max() ? 0.0 : std::chrono::duration<double>(last - first).count();
     return st;
+}
+
+int rmq_serve_serial_loop(rmq_handle* const* handles, uint64_t num_handles, const rmq_trace_event* ev,
+                          uint64_t count, const uint32_t* h_lr, uint32_t* h_argmin, float* h_min, double* wall_s) {
+    if (handles == nullptr || (count > 0 && (ev == nullptr || h_lr == nullptr || h_argmin == nullptr)))
+        return RMQ_ERR_ARG;
+    const Clock::time_point t0 = Clock::now();
+    int first_error = RMQ_OK;
+    for (uint64_t i = 0; i < count; ++i) {
+        if (ev[i].kind != 0) continue;
+        if (ev[i].array_id >= num_handles || handles[ev[i].array_id] == nullptr) return RMQ_ERR_ARG;
+        const uint64_t o = ev[i].q_offset;
+        const int st = rmq_query_idx_host(handles[ev[i].array_id], h_lr + 2 * o, ev[i].q, h_argmin + o,
+                                          h_min != nullptr ? h_min + o : nullptr);
+        if (st != RMQ_OK && first_error == RMQ_OK) first_error = st;
+    }
+    if (wall_s != nullptr) *wall_s = std::chrono::duration<double>(Clock::now() - t0).count();
+    return first_error;
+}
+
+int rmq_server_fail_next_batches(rmq_server* s, uint32_t count) {
+    if (s == nullptr) return RMQ_ERR_ARG;
+    std::lock_guard<std::mutex> lock(s->mu);
+    s->fail_batches = count;
+    return RMQ_OK;
 }
 
 int rmq_server_get_stats(rmq_server* s, rmq_server_stats* stats) {

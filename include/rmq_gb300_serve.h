@@ -78,8 +78,9 @@ int rmq_server_register_host(rmq_server* s, const float* h_values, uint64_t n, u
 int rmq_server_submit(rmq_server* s, uint64_t array_id, const uint32_t* h_lr, uint64_t q, uint32_t* h_argmin,
                       float* h_min, uint64_t* request_id);
 
-/* Waits for a request: its status (RMQ_OK, or RMQ_ERR_QUERY_RANGE when a
- * query was invalid), or RMQ_ERR_TIMEOUT when it is not done within
+/* Waits for a request: its status (RMQ_OK; RMQ_ERR_QUERY_RANGE when a
+ * query was invalid; RMQ_ERR_CUDA when its batch could not be launched, its
+ * argmin then all ones and its minima NaN), or RMQ_ERR_TIMEOUT when it is not done within
  * timeout_ms (< 0: no limit).  *latency_us (may be NULL): submit to results
  * in the host buffers.  A call that returns the status collects the request:
  * the server drops its record and the id is then unknown (RMQ_ERR_ARG);
@@ -99,6 +100,23 @@ int rmq_server_replay(rmq_server* s, const rmq_trace_event* events, uint64_t cou
                       uint32_t* h_argmin, float* h_min, double* latency_us, double* wall_s);
 
 int rmq_server_get_stats(rmq_server* s, rmq_server_stats* stats);
+
+/* The comparator of the server: the query requests (kind 0) of `events`
+ * answered one after another, each by rmq_query_idx_host on a prebuilt
+ * handle of its array (handles[array_id], num_handles of them) and waited for
+ * before the next one starts: a caller's per-request loop of the plain
+ * kernel, without batching or overlap.  Arrival times are ignored; results
+ * land at the same positions as rmq_server_replay's.  *wall_s (may be NULL):
+ * time of the whole loop.  Returns the first failing call's status. */
+int rmq_serve_serial_loop(rmq_handle* const* handles, uint64_t num_handles, const rmq_trace_event* events,
+                          uint64_t count, const uint32_t* h_lr, uint32_t* h_argmin, float* h_min, double* wall_s);
+
+/* Fault injection for tests of the failure path: the next `count` batches
+ * the dispatcher packs fail as if their upload had returned a CUDA error
+ * (nothing of theirs is issued to the device); their requests complete with
+ * RMQ_ERR_CUDA.  count = 0 cancels what is left.  Made on the host: no
+ * device work fails. */
+int rmq_server_fail_next_batches(rmq_server* s, uint32_t count);
 
 /* Stops the dispatcher (after finishing queued work) and frees everything. */
 void rmq_server_destroy(rmq_server* s);

@@ -1,7 +1,7 @@
 """Failure paths on the device side, made on the host (GPU): allocation
 failures reported as RMQ_ERR_OOM with nothing left behind, HBM-budget
-exhaustion in the server, a poisoned request among healthy ones, and a
-bounded wait that gives up.  Nothing here faults, traps or hangs the GPU:
+exhaustion in the server, a poisoned request among healthy ones, a batch
+whose launch fails (injected on the host) and a bounded wait that gives up.  Nothing here faults, traps or hangs the GPU:
 every allocation that fails does so before any kernel could touch the
 (deliberately small) input buffers."""
 from __future__ import annotations
@@ -114,3 +114,30 @@ def test_server_wait_gives_up_then_completes(cuda):
         assert st == R.RMQ_OK and lat > 0
     samp = np.arange(0, qs.shape[0], 97)
     assert np.array_equal(oi[samp], oracle.rmq_argmin(a, qs[samp]))
+
+
+def test_server_failed_batch_reports_cuda_error_to_its_waiter(cuda):
+    """A batch whose launch fails completes its requests with RMQ_ERR_CUDA
+    (argmin all ones, minima NaN), the status set together with completion so
+    a waiter woken at once sees it; the server then keeps serving."""
+    rng = np.random.default_rng(11)
+    a = rng.random(1 << 16).astype(np.float32)
+    with R.Server(hbm_budget_bytes=64 << 20, slots=2) as srv:
+        aid = srv.register_host(a)
+        qs = _queries(rng, a.size, 4000)
+        warm = np.empty(qs.shape[0], np.uint32)
+        assert srv.wait(srv.submit(aid, qs, warm, None))[0] == R.RMQ_OK  # array built
+        srv.fail_next_batches(1)
+        oi = np.zeros(qs.shape[0], np.uint32)
+        om = np.zeros(qs.shape[0], np.float32)
+        st, _ = srv.wait(srv.submit(aid, qs, oi, om))
+        assert st == R.RMQ_ERR_CUDA
+        assert np.all(oi == R.NO_POS) and np.all(np.isnan(om))
+        for _ in range(3):  # the failed batch left nothing behind
+            oi2 = np.empty(qs.shape[0], np.uint32)
+            om2 = np.empty(qs.shape[0], np.float32)
+            st, _ = srv.wait(srv.submit(aid, qs, oi2, om2))
+            assert st == R.RMQ_OK
+            assert np.array_equal(oi2, oracle.rmq_argmin(a, qs))
+            assert om2.tobytes() == oracle.rmq_min(a, qs).tobytes()
+        assert srv.stats()["requests_done"] == 5
