@@ -5,12 +5,22 @@
 // pool (a further cudaMalloc fails or fragments that pool), and latency-bound
 // callers for whom cudaMalloc / cudaFree are off limits because those calls
 // can block and synchronise the device.  For them this file keeps the
-// hierarchy's coarse levels in one file-scope device array of fixed size,
-// allocated when the library's code is loaded on a device and held until the
-// process exits.  The caller still provides the values, the queries and the
-// output buffers.
+// hierarchy's coarse levels in one file-scope device array of fixed size.
+// The caller still provides the values, the queries and the output buffers.
+//
+// When the array exists on a device: CUDA loads device code lazily by default
+// (CUDA_MODULE_LOADING=LAZY), so the array, and the build and query kernels
+// this entry point launches, are placed on a device by the first call made
+// on it, not when the library is loaded.  That first call can therefore need
+// device memory for the array and the kernels' code; a caller that is about
+// to reserve the whole device should make one call (q = 0 is enough for the
+// array and the build kernel; q > 0 also loads the query kernel) before
+// reserving it, and before any stream capture.  From then on the device holds
+// the array until its context is destroyed (process exit or cudaDeviceReset).
 #include <cstring>
 #include <mutex>
+
+#include <cuda.h>  // CUcontext / CUresult types only; the driver calls are looked up at run time
 
 #include "../../include/rmq_gb300.h"
 #include "rmq_internal.h"
@@ -29,25 +39,68 @@ constexpr int kMaxDevices = 64;
 static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 
 // Host code cannot use g_scratch's name as a device address (on the host it
-// names a stand-in object); the device address is looked up once per device.
+// names a stand-in object); its device address is looked up at set-up, once
+// per device context, with that context current.  A context is told apart by
+// its id (cuCtxGetId), so a device reset, which destroys the context and
+// reloads the array elsewhere in a new one, is followed by a fresh lookup
+// rather than a stale address.
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+
+struct ScratchAddr {
+    unsigned long long ctx_id = 0;
+    bool set = false;
+    void* ptr = nullptr;
+};
+
 std::mutex g_setup_mu;
-void* g_scratch_ptr[kMaxDevices] = {};
+ScratchAddr g_scratch_addr[kMaxDevices];
+CtxGetCurrentFn g_ctx_get_current = nullptr;
+CtxGetIdFn g_ctx_get_id = nullptr;
+
+bool current_context_id(unsigned long long* id) {
+    if (g_ctx_get_current == nullptr || g_ctx_get_id == nullptr) {
+        void* f1 = nullptr;
+        void* f2 = nullptr;
+        cudaDriverEntryPointQueryResult q1, q2;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) != cudaSuccess ||
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) != cudaSuccess ||
+            q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || f1 == nullptr ||
+            f2 == nullptr) {
+            cudaGetLastError();
+            return false;
+        }
+        g_ctx_get_current = reinterpret_cast<CtxGetCurrentFn>(f1);
+        g_ctx_get_id = reinterpret_cast<CtxGetIdFn>(f2);
+    }
+    CUcontext ctx = nullptr;
+    if (g_ctx_get_current(&ctx) != CUDA_SUCCESS || ctx == nullptr) return false;
+    return g_ctx_get_id(ctx, id) == CUDA_SUCCESS;
+}
 
 int scratch_for_current_device(void** out) {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return RMQ_ERR_CUDA;
     if (dev < 0 || dev >= kMaxDevices) return RMQ_ERR_UNSUPPORTED;
     std::lock_guard<std::mutex> lock(g_setup_mu);
-    if (g_scratch_ptr[dev] == nullptr) {
+    ScratchAddr& slot = g_scratch_addr[dev];
+    unsigned long long id = 0;
+    // Before the runtime has made a context current on this thread there is
+    // no id to compare: the lookup below makes it current.
+    const bool have_id = current_context_id(&id);
+    if (!slot.set || !have_id || slot.ctx_id != id) {
         void* p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
         if (e != cudaSuccess || p == nullptr) {
             cudaGetLastError();
             return RMQ_ERR_CUDA;
         }
-        g_scratch_ptr[dev] = p;
+        if (!current_context_id(&id)) return RMQ_ERR_CUDA;
+        slot.ctx_id = id;
+        slot.ptr = p;
+        slot.set = true;
     }
-    *out = g_scratch_ptr[dev];
+    *out = slot.ptr;
     return RMQ_OK;
 }
 

@@ -8,8 +8,10 @@ library holds on each device, the caller passes only inputs and outputs.
 
 Checked through the C ABI against the handle-based rmq_query_idx, bit for
 bit, on two calls in a row (a larger array first, so stale coarse levels
-from the first call would show up in the second).  This file is collected
-last so that a stopping run has already run every other test.
+from the first call would show up in the second), with a non-default scan
+threshold, with no queries, and with invalid queries; and that a call leaves
+the device's free memory unchanged.  This file is collected last so that a
+stopping run has already run every other test.
 """
 from __future__ import annotations
 
@@ -63,3 +65,61 @@ def test_static_rejects_sizes_beyond_the_limit(cuda):
     out = torch.empty(1, dtype=torch.int32, device=cuda)
     st = f(dv.data_ptr(), n, 0, dq.data_ptr(), 1, out.data_ptr(), None, None)
     assert st == R.RMQ_ERR_UNSUPPORTED
+
+
+def _handle_results(cuda, dv, dq, t):
+    with R.Hierarchy(dv, variant="vl", t=t, rf_log=3) as h:
+        return h.query_idx(dq, with_min=True)
+
+
+def test_static_other_threshold_empty_and_invalid_queries(cuda):
+    import torch
+    f = _entry()
+    n, q = 1 << 20, 1 << 16
+    a = R.gen_array(n, 21)
+    qs = R.gen_queries(q, -1, n, 21)
+    qs[5] = (100, 50)        # l > r
+    qs[q - 1] = (0, n)       # r = n
+    dv = torch.from_numpy(a).to(cuda)
+    dq = torch.from_numpy(qs.view(np.int32)).to(cuda)
+    exp_i, exp_m = _handle_results(cuda, dv, dq, 8)
+    got_i = torch.zeros(q, dtype=torch.int32, device=cuda)
+    got_m = torch.zeros(q, dtype=torch.float32, device=cuda)
+    st = f(dv.data_ptr(), n, 8, dq.data_ptr(), q, got_i.data_ptr(), got_m.data_ptr(), None)
+    assert st == R.RMQ_OK, R.strerror(st)
+    torch.cuda.synchronize()
+    assert torch.equal(got_i, exp_i) and torch.equal(got_m.view(torch.int32), exp_m.view(torch.int32))
+    gi = got_i.cpu().numpy().view(np.uint32)
+    gm = got_m.cpu().numpy()
+    assert gi[5] == R.NO_POS and gi[q - 1] == R.NO_POS and np.isnan(gm[5]) and np.isnan(gm[q - 1])
+    keep = np.ones(q, bool)
+    keep[[5, q - 1]] = False
+    from oracle import oracle
+    assert np.array_equal(gi[keep], oracle.rmq_argmin(a, qs[keep]))
+    # no queries: nothing is written
+    sentinel = torch.full((4,), 7, dtype=torch.int32, device=cuda)
+    assert f(dv.data_ptr(), n, 0, None, 0, sentinel.data_ptr(), None, None) == R.RMQ_OK
+    torch.cuda.synchronize()
+    assert torch.equal(sentinel, torch.full((4,), 7, dtype=torch.int32, device=cuda))
+
+
+def test_static_call_leaves_free_device_memory_unchanged(cuda):
+    import torch
+    f = _entry()
+    n, q = 1 << 22, 1 << 18
+    a = R.gen_array(n, 31)
+    qs = R.gen_queries(q, -6, n, 31)
+    dv = torch.from_numpy(a).to(cuda)
+    dq = torch.from_numpy(qs.view(np.int32)).to(cuda)
+    oi = torch.empty(q, dtype=torch.int32, device=cuda)
+    om = torch.empty(q, dtype=torch.float32, device=cuda)
+    # The first call on a device may load the array and the kernels; after it,
+    # a call must not change the free memory.
+    assert f(dv.data_ptr(), n, 0, dq.data_ptr(), q, oi.data_ptr(), om.data_ptr(), None) == R.RMQ_OK
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info(cuda)
+    for _ in range(3):
+        assert f(dv.data_ptr(), n, 0, dq.data_ptr(), q, oi.data_ptr(), om.data_ptr(), None) == R.RMQ_OK
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info(cuda)
+    assert free1 == free0
