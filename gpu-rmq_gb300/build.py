@@ -9,8 +9,8 @@ units in parallel, one -gencode (sm_103a).  Outputs:
   gpu-rmq_gb300/librmq_gen.so        host input generators (include/rmq_gb300_gen.h)
   gpu-rmq_gb300/driver/rtxrmq        the benchmark driver (reference CLI)
   oracle/liboracle.so                CPU oracle (test infrastructure)
-  oracle/_ref/librmq_ref.so          reference build for pinning (only where
-                                     the reference sources exist)
+  oracle/_ref/librmq_ref.so          reference build for pinning (only when
+                                     RMQ_REFERENCE_ROOT names the reference checkout)
 """
 from __future__ import annotations
 
@@ -33,7 +33,7 @@ BUILD = PKG / "_build" / platform.machine()
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 CUDA_SOURCES = ["rmq_build.cu", "rmq_query.cu", "rmq_api.cu", "rmq_noalloc.cu", "rmq_batch.cu",
-                "rmq_gen_device.cu", "rmq_serve.cu"]
+                "rmq_gen_device.cu", "rmq_serve.cu", "rmq_probe.cu"]
 
 LIB = PKG / "librmq_gb300.so"
 CHECKED_LIB = PKG / "librmq_gb300_checked.so"  # bounds-checked build (tests only)
@@ -131,15 +131,24 @@ def build_driver(force: bool = False) -> Path:
 
 
 def build_oracle(force: bool = False) -> Path:
-    src = ORACLE / "rmq_oracle.c"
-    if force or _stale(ORACLE_LIB, [src]):
-        _run(["gcc", "-O2", "-std=c11", "-fPIC", "-fopenmp", "-shared", str(src), "-o", str(ORACLE_LIB)])
+    """The oracle (C scan and sparse table, C++ generators) as one library."""
+    src_c, src_cpp = ORACLE / "rmq_oracle.c", ORACLE / "rmq_oracle_gen.cpp"
+    if force or _stale(ORACLE_LIB, [src_c, src_cpp]):
+        BUILD.mkdir(parents=True, exist_ok=True)
+        obj_c, obj_cpp = BUILD / "rmq_oracle.o", BUILD / "rmq_oracle_gen.o"
+        _run(["gcc", "-O2", "-std=c11", "-fPIC", "-fopenmp", "-c", str(src_c), "-o", str(obj_c)])
+        _run(["g++", "-O2", "-std=c++17", "-fPIC", "-c", str(src_cpp), "-o", str(obj_cpp)])
+        _run(["g++", "-shared", "-fopenmp", str(obj_c), str(obj_cpp), "-o", str(ORACLE_LIB)])
     return ORACLE_LIB
 
 
 def build_reference(force: bool = False) -> Path | None:
-    """Compiles the reference's own CPU path for pinning, when its sources exist."""
-    ref = Path(os.environ.get("RMQ_REFERENCE_ROOT", "/root/reference"))
+    """Compiles the reference's own CPU path for pinning, when the environment
+    variable RMQ_REFERENCE_ROOT names a reference checkout."""
+    root = os.environ.get("RMQ_REFERENCE_ROOT")
+    if not root:
+        return None
+    ref = Path(root)
     if not (ref / "src" / "cpu_methods.h").exists():
         return None
     deps = [ORACLE / "ref_harness.cu", ORACLE / "ref_gpu_harness.cu", ORACLE / "build_ref.sh"]

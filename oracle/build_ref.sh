@@ -2,7 +2,8 @@
 # Builds oracle/_ref/librmq_ref.so from the reference's own sources (read in
 # place, never copied) for pinning the oracle.  TEST INFRASTRUCTURE ONLY.
 #
-# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default: /root/reference)
+# Usage: oracle/build_ref.sh REFERENCE_ROOT
+#    or: RMQ_REFERENCE_ROOT=<reference checkout> oracle/build_ref.sh
 #
 # The reference's CPU path (src/cpu_methods.h) #includes the header of an
 # external CPU RMQ library that the reference does not vendor
@@ -11,7 +12,11 @@
 # src/tools.h reads cudaDeviceProp::memoryClockRate, which CUDA 13 removed; it
 # is mapped onto an existing field for compilation (that code is never run).
 set -euo pipefail
-REF="${1:-/root/reference}"
+REF="${1:-${RMQ_REFERENCE_ROOT:-}}"
+if [ -z "$REF" ]; then
+    echo "build_ref: name the reference checkout (argument or RMQ_REFERENCE_ROOT); nothing built" >&2
+    exit 0
+fi
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"
 if [ ! -d "$REF/src" ]; then

@@ -5,7 +5,9 @@ module, and only as the checker or as the timed CPU baseline.
 
   liboracle.so        restatement of the reference's brute-force scan
                       (src/cpu_methods.h:7-77) plus a sparse-table oracle and
-                      the level-layout rule (src/xxx.h:225-243); see rmq_oracle.c
+                      the level-layout rule (src/xxx.h:225-243), rmq_oracle.c;
+                      and of its input generators (src/rand.cuh:49-240),
+                      rmq_oracle_gen.cpp
   _ref/librmq_ref.so  the reference's own generator and CPU scan, compiled from
                       its sources by build_ref.sh where they are present
 """
@@ -40,6 +42,12 @@ def lib() -> ctypes.CDLL:
         L.oracle_sparse_free.argtypes = [_P]
         L.oracle_sparse_query.argtypes = [_P, _P, _U64, _P, _P, ctypes.c_int]
         L.oracle_layout.argtypes = [_U64, _U64, ctypes.c_int, _P, _P, _P]
+        L.oracle_cpu_rmq.argtypes = [_P, _P, _U64, _P, ctypes.c_int]
+        L.oracle_cpu_rmq_idx.argtypes = [_P, _P, _U64, _P, ctypes.c_int]
+        L.oracle_gen_array.argtypes = [_U64, ctypes.c_int32, _P]
+        L.oracle_gen_queries.argtypes = [_U64, ctypes.c_int32, _U64, ctypes.c_int32, _P]
+        L.oracle_gen_queries.restype = ctypes.c_int32
+        L.oracle_plant_min_ties.argtypes = [_P, _U64, ctypes.c_double, ctypes.c_int32]
         _o = L
     return _o
 
@@ -88,6 +96,44 @@ def rmq_argmin(a: np.ndarray, qs: np.ndarray, nthreads: int = 0) -> np.ndarray:
     out = np.empty(q, dtype=np.uint32)
     lib().oracle_argmin(_c(a), a.size, _c(qs), q, _c(out), nthreads)
     return out
+
+
+def cpu_rmq(a: np.ndarray, qs: np.ndarray, nthreads: int = 0) -> np.ndarray:
+    """cpu_rmq as the reference runs it (default OpenMP schedule); valid
+    queries only.  The timed CPU baseline."""
+    q = qs.size // 2
+    out = np.empty(q, dtype=np.float32)
+    lib().oracle_cpu_rmq(_c(a), _c(qs), q, _c(out), nthreads)
+    return out
+
+
+def cpu_rmq_idx(a: np.ndarray, qs: np.ndarray, nthreads: int = 0) -> np.ndarray:
+    """cpu_rmq_idx as the reference runs it; valid queries only."""
+    q = qs.size // 2
+    out = np.empty(q, dtype=np.uint32)
+    lib().oracle_cpu_rmq_idx(_c(a), _c(qs), q, _c(out), nthreads)
+    return out
+
+
+def gen_array(n: int, seed: int) -> np.ndarray:
+    """The reference's random_array_par_cpu (src/rand.cuh:49-61)."""
+    a = np.empty(n, dtype=np.float32)
+    lib().oracle_gen_array(n, seed, _c(a))
+    return a
+
+
+def gen_queries(q: int, lr: int, n: int, seed: int) -> np.ndarray:
+    """The reference's random_queries_par_cpu (src/rand.cuh:181-217) and the
+    added laws -7 / -8, as inclusive [q, 2] uint32 pairs."""
+    out = np.empty((q, 2), dtype=np.uint32)
+    if lib().oracle_gen_queries(q, lr, n, seed, _c(out)) != 0:
+        raise ValueError(f"unknown length law lr={lr} for n={n}")
+    return out
+
+
+def plant_min_ties(a: np.ndarray, frac: float, seed: int) -> np.ndarray:
+    lib().oracle_plant_min_ties(_c(a), a.size, frac, seed)
+    return a
 
 
 class Sparse:

@@ -12,6 +12,9 @@
  * produced by that build (tests/golden/).
  *
  * Contents
+ *   oracle_cpu_rmq / _idx        cpu_rmq / cpu_rmq_idx as the reference runs
+ *                                them (default OpenMP schedule): the timed
+ *                                CPU baseline
  *   oracle_min / oracle_argmin   restatement of cpu_min / cpu_min_idx
  *                                (src/cpu_methods.h:7-16, :42-53) run over a
  *                                query batch as cpu_rmq / cpu_rmq_idx do
@@ -58,7 +61,9 @@ static uint32_t scan_argmin(const float* A, uint32_t l, uint32_t r) {
 
 /* Q holds q inclusive pairs {l, r}.  Invalid pairs (l > r or r >= n) produce
  * NaN / 0xFFFFFFFF, the library's convention for invalid queries (the
- * reference does not check and reads out of bounds). */
+ * reference does not check and reads out of bounds).  The checker: queries
+ * are dealt out dynamically (64 at a time), which keeps the threads busy on
+ * mixed lengths. */
 void oracle_min(const float* A, uint64_t n, const uint32_t* Q, uint64_t q, float* out, int nthreads) {
 #ifdef _OPENMP
     if (nthreads > 0) omp_set_num_threads(nthreads);
@@ -90,6 +95,28 @@ void oracle_argmin(const float* A, uint64_t n, const uint32_t* Q, uint64_t q, ui
         }
         out[i] = scan_argmin(A, l, r);
     }
+    (void)nthreads;
+}
+
+/* cpu_rmq / cpu_rmq_idx as the reference runs them (src/cpu_methods.h:18-39,
+ * :55-77): one OpenMP parallel for over the queries with the default
+ * schedule, each query a cpu_min / cpu_min_idx scan.  The timed CPU baseline;
+ * valid queries only (the reference does not check them). */
+void oracle_cpu_rmq(const float* A, const uint32_t* Q, uint64_t q, float* out, int nthreads) {
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for
+#endif
+    for (int64_t i = 0; i < (int64_t)q; ++i) out[i] = scan_min(A, Q[2 * i], Q[2 * i + 1]);
+    (void)nthreads;
+}
+
+void oracle_cpu_rmq_idx(const float* A, const uint32_t* Q, uint64_t q, uint32_t* out, int nthreads) {
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for
+#endif
+    for (int64_t i = 0; i < (int64_t)q; ++i) out[i] = scan_argmin(A, Q[2 * i], Q[2 * i + 1]);
     (void)nthreads;
 }
 

@@ -272,12 +272,13 @@ def test_full_size_large_mixed_ties(cuda):
 
 @pytest.mark.parametrize("n", [1025 * 8192, 1025 * 8192 + 5, 3 * (1 << 22) + 13, (1 << 24) + 8191])
 def test_streamed_build_sizes(cuda, n):
-    """Arrays of more than 1024 tiles of 8192 entries, whose level 0 streams
-    through shared memory by bulk copy (whole tiles) plus a global-load pass
-    for a partial last tile: every tile's block minima, heavy ties and signed
-    zeros, with queries spanning each tile, crossing each tile boundary and of
-    random lengths, against the GPU brute-force checker, for every reduction
-    factor and both variants at their smallest t (every level is read)."""
+    """Arrays of more than 1024 tiles of 8192 entries, where the fused build
+    kernel leaves the levels above its tiles to the tail and step kernels,
+    some with a partial last tile: every tile's block minima, heavy ties and
+    signed zeros, with queries spanning each tile, crossing each tile boundary
+    and of random lengths, against the GPU brute-force checker, for every
+    reduction factor and both variants at their smallest t (every level is
+    read)."""
     import torch
     rng = np.random.default_rng(n)
     a = rng.integers(-50, 50, n).astype(np.float32)
