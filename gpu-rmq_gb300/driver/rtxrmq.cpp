@@ -66,6 +66,10 @@ struct Args {
     std::string variant = "auto";
     int rf_log = 0, lanes = 0, l2_persist = 0;
     double ties = 0.0;
+    uint64_t nb = 0;               // --nb as given (0 = not given)
+    int log_build_threshold = 0;   // accepted and recorded; no effect here
+    int save_power = 0;            // accepted; power is not measured
+    double hbm_peak = 0.0;         // GB/s for roofline_frac (0 = device theoretical)
 };
 
 const char* alg_name(int alg) {
@@ -82,40 +86,44 @@ const char* alg_name(int alg) {
 
 void print_help() {
     std::fprintf(stderr,
-                 "run as ./rtxrmq <n> <q> <lr> <alg>\n\n"
-                 "n   = num elements\n"
-                 "q   = num RMQ queries\n"
-                 "lr  = length of range; min 1, max n\n"
-                 "  >0 -> value\n"
-                 "  -1 -> uniform distribution (large values)\n"
-                 "  -2 -> lognormal distribution (medium values)\n"
-                 "  -3 -> lognormal distribution (small values)\n"
-                 "  -4, -5 -> lognormal, median n/2^8, n/2^15\n"
-                 "  -6 -> mixed distribution (large, medium and small values)\n"
-                 "  -7 -> lognormal, median 2^13, sigma 1.0 (clamped)\n"
-                 "  -8 -> thirds of uniform, lognormal(2^13, 1.0), lognormal(2^5, 0.7)\n"
-                 "alg = algorithm\n"
-                 "    0 -> [CPU] BASE\n"
-                 "    2 -> [GPU] BASE\n"
-                 "   22 -> [GPU] GB300 hierarchical (CL/VL work distributions)\n"
-                 "  100, 102, 122 -> algs 0 2 22 returning indices\n\n"
-                 "Options:\n"
-                 "   --log_bs <t>              scan threshold t of alg 22, as log2 (default 15, clamped to log2 n)\n"
-                 "   --reps <repetitions>      RMQ repeats for the avg time (default: 10)\n"
-                 "   --dev <device ID>         device ID (default: 0)\n"
-                 "   --nt <thread num>         number of CPU threads\n"
-                 "   --seed <seed>             seed for PRNG\n"
-                 "   --check                   check every query against the GPU brute-force scan (bit-exact)\n"
-                 "   --trivialCheck            2^10 distinct queries repeated to q, checked\n"
-                 "   --randTrivialCheck        check 2^15 randomly sampled queries\n"
-                 "   --save-time[=<file>]      append a CSV row\n"
-                 "   --save-input-data         cache arrays, queries and expected results as raw binaries\n"
-                 "   --data-dir <dir>          directory of that cache (default: .)\n"
-                 "   --variant cl|vl|auto      work distribution of alg 22/122 (default: auto)\n"
-                 "   --rf_log <3..5>           log2 of the reduction factor (default: variant's)\n"
-                 "   --lanes <2|4|8|16|32>     CL lanes per query\n"
-                 "   --l2_persist              keep the coarse levels in an L2 persisting window\n"
-                 "   --ties <frac>             set that fraction of entries to the global minimum\n");
+                 "usage: ./rtxrmq <n> <q> <lr> <alg> [options]\n\n"
+                 "  n    size of the fp32 array\n"
+                 "  q    number of range-minimum queries\n"
+                 "  lr   query length law (a length is between 1 and n):\n"
+                 "         lr > 0  every query has length lr\n"
+                 "         -1      length uniform over [1, n]\n"
+                 "         -2, -3  lognormal lengths around n^0.6 / n^0.3 (sigma 0.3)\n"
+                 "         -4, -5  lognormal lengths around n/2^8 / n/2^15 (sigma 0.3)\n"
+                 "         -6      a random pick of -1, -2 or -3 per query\n"
+                 "         -7      lognormal around 2^13 with sigma 1.0, clamped to [1, n]\n"
+                 "         -8      thirds of: -1, lognormal(2^13, 1.0), lognormal(2^5, 0.7)\n"
+                 "  alg  what answers the queries:\n"
+                 "          0  CPU brute-force scan (OpenMP)\n"
+                 "          2  GPU brute-force scan\n"
+                 "         22  GPU hierarchy of block minima for GB300 (--variant cl|vl|auto)\n"
+                 "         100, 102, 122: the same three returning the position of the minimum\n\n"
+                 "options:\n"
+                 "  --log_bs <k>            alg 22/122: scan threshold t = 2^k (default 2^15, at most n)\n"
+                 "  --nb <blocks>           alg 22/122: t from a block count, t = 2^ceil(log2(n / blocks))\n"
+                 "  --reps <r>              timed repetitions (default 10)\n"
+                 "  --dev <id>              CUDA device (default 0)\n"
+                 "  --nt <threads>          CPU threads of alg 0/100\n"
+                 "  --seed <s>              generator seed (default: the clock)\n"
+                 "  --check                 compare every result with the GPU brute-force scan, bit for bit\n"
+                 "  --trivialCheck          only 2^10 distinct queries, repeated up to q, all compared\n"
+                 "  --randTrivialCheck      compare a random sample of 2^15 results\n"
+                 "  --save-time[=<file>]    append one CSV row of results (default ../results/data.csv)\n"
+                 "  --save-input-data       keep generated inputs and expected results as raw files\n"
+                 "  --data-dir <dir>        where those files go (default .)\n"
+                 "  --log_build_threshold[=<k>]  accepted for command-line compatibility (no effect here)\n"
+                 "  --save-power[=<file>]   accepted for command-line compatibility (power is not measured)\n"
+                 "  --variant cl|vl|auto    work distribution of alg 22/122 (default auto)\n"
+                 "  --rf_log <3..5>         log2 of the per-level reduction factor (default: the variant's)\n"
+                 "  --lanes <2|4|8|16|32>   CL lanes per query\n"
+                 "  --l2_persist            put the coarse levels in an L2 persisting window\n"
+                 "  --ties <frac>           set that fraction of the entries to the array's minimum\n"
+                 "  --hbm_peak <GB/s>       peak for the CSV roofline_frac column (default: the device's\n"
+                 "                          theoretical rate from its memory clock and bus width)\n");
 }
 
 bool parse(int argc, char** argv, Args& a) {
@@ -143,7 +151,7 @@ bool parse(int argc, char** argv, Args& a) {
     }
     a.seed = int(std::time(nullptr));
     enum { O_BS = 1, O_REPS, O_DEV, O_NT, O_SEED, O_CHECK, O_TRIV, O_RTRIV, O_TIME, O_SAVE, O_DIR,
-           O_VAR, O_RF, O_LANES, O_L2, O_TIES };
+           O_VAR, O_RF, O_LANES, O_L2, O_TIES, O_NB, O_THRESH, O_POWER, O_PEAK };
     static option opts[] = {
         {"log_bs", required_argument, nullptr, O_BS},
         {"reps", required_argument, nullptr, O_REPS},
@@ -161,6 +169,10 @@ bool parse(int argc, char** argv, Args& a) {
         {"lanes", required_argument, nullptr, O_LANES},
         {"l2_persist", no_argument, nullptr, O_L2},
         {"ties", required_argument, nullptr, O_TIES},
+        {"nb", required_argument, nullptr, O_NB},
+        {"log_build_threshold", optional_argument, nullptr, O_THRESH},
+        {"save-power", optional_argument, nullptr, O_POWER},
+        {"hbm_peak", required_argument, nullptr, O_PEAK},
         {nullptr, 0, nullptr, 0}};
     int opt, idx;
     optind = 5;
@@ -192,6 +204,29 @@ bool parse(int argc, char** argv, Args& a) {
             case O_LANES: a.lanes = std::atoi(optarg); break;
             case O_L2: a.l2_persist = 1; break;
             case O_TIES: a.ties = std::atof(optarg); break;
+            case O_NB: {
+                // as the reference (src/tools.h:168-175): nb = min(n, blocks),
+                // t = 2^ceil(log2(n / nb)); a later --log_bs overrides it
+                const long long v = std::atoll(optarg);
+                if (v <= 0) {
+                    std::fprintf(stderr, "Error: --nb needs a positive block count\n");
+                    return false;
+                }
+                a.nb = std::min<uint64_t>(a.n, uint64_t(v));
+                const uint64_t per = a.n / a.nb;
+                uint32_t lg = 0;
+                while ((uint64_t(1) << lg) < per) ++lg;
+                a.log_bs = lg;
+                break;
+            }
+            case O_THRESH:
+                if (optarg) a.log_build_threshold = std::atoi(optarg);
+                break;
+            case O_POWER:
+                a.save_power = 1;
+                std::fprintf(stderr, "note: --save-power is accepted but power is not measured by this driver\n");
+                break;
+            case O_PEAK: a.hbm_peak = std::atof(optarg); break;
             default: print_help(); return false;
         }
     }
@@ -273,6 +308,41 @@ void save_raw(const std::string& f, const void* src, size_t bytes) {
     }
     std::fwrite(src, 1, bytes, fp);
     std::fclose(fp);
+}
+
+// Algorithmic bytes of one query (the implementation-independent model the
+// benchmark reports as roofline.achieved): the canonical descent with rf = 32
+// reads, at level 0, the 32-byte sectors of [l, r] when the range has at most
+// 64 entries, else those of [l, ceil32(l)) and [floor32(r + 1), r + 1).
+uint64_t level0_sectors(uint64_t l, uint64_t r, uint64_t n) {
+    const uint64_t e = r + 1, rf = 32;
+    if (e - l <= 2 * rf || n <= 64) return (r >> 3) - (l >> 3) + 1;
+    const uint64_t nl = (l + rf - 1) & ~(rf - 1), pr = e & ~(rf - 1);
+    const uint64_t left = nl > l ? ((nl - 1) >> 3) - (l >> 3) + 1 : 0;
+    const uint64_t right = e > pr ? (r >> 3) - (pr >> 3) + 1 : 0;
+    return left + right;
+}
+
+// Sectors of levels >= 1 the same canonical descent (rf = 32, t = 64) reads:
+// boundary pieces while it descends, then its final piece.
+uint64_t coarse_sectors(uint64_t l, uint64_t r, uint64_t n) {
+    const uint64_t rf = 32, t = 64;
+    uint32_t top = 0;
+    for (uint64_t size = n; top < 19 && size > t; size = (size + rf - 1) / rf) ++top;
+    uint64_t lo = l, e = r + 1, total = 0;
+    uint32_t k = 0;
+    while (k < top && e - lo > 2 * rf) {
+        const uint64_t nl = (lo + rf - 1) & ~(rf - 1), pr = e & ~(rf - 1);
+        if (k > 0) {
+            if (nl > lo) total += ((nl - 1) >> 3) - (lo >> 3) + 1;
+            if (e > pr) total += ((e - 1) >> 3) - (pr >> 3) + 1;
+        }
+        lo = nl / rf;
+        e = pr / rf;
+        ++k;
+    }
+    if (k > 0 && e > lo) total += ((e - 1) >> 3) - (lo >> 3) + 1;
+    return total;
 }
 
 struct Result {
@@ -442,7 +512,7 @@ int check(const Args& a, const float* hA, const uint32_t* hQ, const float* dA, c
     return wrong == 0 ? 1 : 0;
 }
 
-void write_csv(const Args& a, const Result& r, int check_code) {
+void write_csv(const Args& a, const Result& r, const uint32_t* hQ, int check_code) {
     if (!a.save_time) return;
     const bool hier = a.alg == ALG_GB300 || a.alg == ALG_GB300_IDX;
     FILE* probe = std::fopen(a.time_file.c_str(), "r");
@@ -453,17 +523,19 @@ void write_csv(const Args& a, const Result& r, int check_code) {
         std::fprintf(stderr, "warning: cannot open %s\n", a.time_file.c_str());
         return;
     }
-    // Column schema of create_XXX_header / create_header (src/tools.h:508-524),
-    // with this driver's columns appended after checkResult.
+    // Column schema of create_XXX_header / create_header (src/tools.h:508-524);
+    // this driver's columns follow checkResult.
+    const char* extra = "variant,rf_log,lanes,event_qps,hbm_GBps,l2_GBps,roofline_frac,p50_us,p99_us,mode,"
+                        "hbm_peak_GBps\n";
     if (!exists) {
         if (hier)
             std::fprintf(fp, "dev,alg,nt,reps,n,bs,nb,q,lr,GPU_BSIZE,CG_GROUP_SIZE,CG_MEM_ALIGNMENT,timestamp,"
                              "scan_threshold,XXX_CG_SIZE_LOG,XXX_CG_AMOUNT_LOG,t,q/s,ns/q,construction,outbuffer,"
-                             "tempbuffer,freeGPUMemCorrect,freeGPUMem,checkResult,variant,rf_log,lanes,event_qps\n");
+                             "tempbuffer,freeGPUMemCorrect,freeGPUMem,checkResult,%s", extra);
         else
             std::fprintf(fp, "dev,alg,nt,reps,n,bs,nb,q,lr,GPU_BSIZE,CG_GROUP_SIZE,CG_MEM_ALIGNMENT,timestamp,t,"
-                             "q/s,ns/q,construction,outbuffer,tempbuffer,freeGPUMemCorrect,freeGPUMem,checkResult,"
-                             "variant,rf_log,lanes,event_qps\n");
+                             "q/s,ns/q,construction,outbuffer,tempbuffer,freeGPUMemCorrect,freeGPUMem,checkResult,%s",
+                         extra);
     }
     char device[300] = "CPU";
     if (is_gpu_alg(a.alg)) {
@@ -481,17 +553,56 @@ void write_csv(const Args& a, const Result& r, int check_code) {
     const int mem_ok = is_gpu_alg(a.alg) && cudaMemGetInfo(&free_b, &total_b) == cudaSuccess ? 1 : 0;
     const double t_it = r.total_ms / a.reps;
     const int gpu_bsize = is_gpu_alg(a.alg) ? 256 : 0;
+    // bs and nb as the reference writes them: 1 and 0 for its hierarchy rows
+    // (src/tools.h:385-392), and for every algorithm whose block size it
+    // resets (src/tools.h:221-235), which covers all of this driver's.
+    const bool vl = r.info.variant == RMQ_VARIANT_VL;
+    int size_log = 0;
+    while (size_log < 6 && (1 << size_log) < r.info.lanes) ++size_log;
+    // XXX_CG_SIZE_LOG: log2 of the lanes per query, 0 for VL (src/tools.h:403);
+    // XXX_CG_AMOUNT_LOG: log2 of the entries per lane and level step, rf / lanes
+    // (CL) or rf / 4 (VL, whose build uses 4-lane tiles, src/xxx.h:1002).
+    const int cg_size_log = vl ? 0 : size_log;
+    const int cg_amount_log = int(r.info.rf_log) - (vl ? 2 : size_log);
     if (hier)
         std::fprintf(fp, "%s,%s,%d,%d,%llu,1,0,%u,%d,%d,0,0,%s,%llu,%d,%d,", device, alg_name(a.alg), a.nt, a.reps,
                      (unsigned long long)a.n, a.q, a.lr, gpu_bsize, ts, (unsigned long long)(uint64_t(1) << a.log_bs),
-                     r.info.lanes, int(r.info.rf_log));
+                     cg_size_log, cg_amount_log);
     else
-        std::fprintf(fp, "%s,%s,%d,%d,%llu,0,0,%u,%d,%d,0,0,%s,", device, alg_name(a.alg), a.nt, a.reps,
+        std::fprintf(fp, "%s,%s,%d,%d,%llu,1,0,%u,%d,%d,0,0,%s,", device, alg_name(a.alg), a.nt, a.reps,
                      (unsigned long long)a.n, a.q, a.lr, gpu_bsize, ts);
-    std::fprintf(fp, "%f,%f,%f,%f,%f,%f,%d,%f,%d,%s,%d,%d,%f\n", r.total_ms / 1000.0, double(a.q) / (t_it / 1000.0),
-                 t_it * 1e6 / a.q, double(r.build_ms), r.out_mb, 0.0, mem_ok, double(free_b) / 1048576.0, check_code,
-                 hier ? a.variant.c_str() : "", hier ? int(r.info.rf_log) : 0, hier ? r.info.lanes : 0,
-                 double(a.q) / (r.event_ms / 1000.0));
+    // outbuffer: the level buffer of block minima (MB), as the reference
+    // (src/xxx.h:269); tempbuffer: the stored argmin positions beside it.
+    const bool idx = is_idx_alg(a.alg);
+    const double lvl_mb = hier ? double(r.info.level_bytes) / 1e6 : 0.0;
+    const double out_mb = idx ? lvl_mb / 2 : lvl_mb, tmp_mb = idx ? lvl_mb / 2 : 0.0;
+    std::fprintf(fp, "%f,%f,%f,%f,%f,%f,%d,%f,%d,", r.total_ms / 1000.0, double(a.q) / (t_it / 1000.0),
+                 t_it * 1e6 / a.q, double(r.build_ms), out_mb, tmp_mb, mem_ok, double(free_b) / 1048576.0,
+                 check_code);
+    std::fprintf(fp, "%s,%d,%d,%f,", hier ? a.variant.c_str() : "", hier ? int(r.info.rf_log) : 0,
+                 hier ? r.info.lanes : 0, double(a.q) / (r.event_ms / 1000.0));
+    if (hier && r.event_ms > 0) {
+        uint64_t b0 = 0, b1 = 0;
+        for (uint64_t i = 0; i < a.q; ++i) {
+            b0 += level0_sectors(hQ[2 * i], hQ[2 * i + 1], a.n);
+            b1 += coarse_sectors(hQ[2 * i], hQ[2 * i + 1], a.n);
+        }
+        const double hbm_bytes = double(a.q) * (8 + 4) + 32.0 * double(b0);
+        const double hbm = hbm_bytes / (r.event_ms / 1e3) / 1e9, l2 = 32.0 * double(b1) / (r.event_ms / 1e3) / 1e9;
+        double peak = a.hbm_peak;
+        if (!(peak > 0)) {
+            int clk_khz = 0, bus_bits = 0;
+            if (cudaDeviceGetAttribute(&clk_khz, cudaDevAttrMemoryClockRate, a.dev) == cudaSuccess &&
+                cudaDeviceGetAttribute(&bus_bits, cudaDevAttrGlobalMemoryBusWidth, a.dev) == cudaSuccess)
+                peak = 2.0 * double(clk_khz) * 1e3 * (bus_bits / 8.0) / 1e9;
+            cudaGetLastError();
+        }
+        std::fprintf(fp, "%f,%f,", hbm, l2);
+        if (peak > 0) std::fprintf(fp, "%f,,,plain,%f\n", hbm / peak, peak);
+        else std::fprintf(fp, ",,,plain,\n");
+    } else {
+        std::fprintf(fp, ",,,,,%s,\n", is_gpu_alg(a.alg) ? "plain" : "cpu");
+    }
     std::fclose(fp);
 }
 
@@ -573,7 +684,7 @@ int main(int argc, char** argv) {
         std::printf("%s\n", pass ? "pass" : "failed");
         check_code = pass + (a.trivial ? 2 : 0) + (a.rand_trivial ? 4 : 0);
     }
-    write_csv(a, r, check_code);
+    write_csv(a, r, hQ.data(), check_code);
     if (dA) cudaFree(dA);
     if (dQ) cudaFree(dQ);
     std::printf("Benchmark Finished\n");
