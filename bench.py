@@ -1,30 +1,47 @@
 #!/usr/bin/env python3
 """Benchmark of the GB300 hierarchical RMQ path.
 
-Workload (N = 1): the plain single-array configuration — n = 2^26 fp32 values
-uniform in [0, 1), q = 2^26 inclusive queries with lengths
+Headline workload (N = 1): the plain single-array configuration — n = 2^26
+fp32 values uniform in [0, 1), q = 2^26 inclusive queries with lengths
 clamp(round(exp(N(ln 2^13, 1))), 1, n) and l uniform in [0, n - len]; every
 query returns its fp32 minimum and its int32 argmin (ties to the lowest
 index).  One step is one pass of the query kernel over all q queries with the
 array, the hierarchy and the queries resident in HBM.  The inputs (1 GiB of
 queries and values, 512 MiB of outputs) exceed the 129 MB L2, so no flush is
-needed between steps (smaller workloads, --n / --q, are timed step by step
-with L2 flushed in between).  The line also carries the roofline of the
-query kernel, the end-to-end figure through rmq_query_idx_host on page-locked
-host buffers, the reference's own GPU kernels timed on the same inputs, the
-CPU baseline and the SM clocks sampled during the timed region.
+needed between steps (smaller workloads are timed step by step with L2
+flushed in between).  The line also carries the roofline of the query
+kernel (HBM, and L2 against an L2 read rate measured here), the end-to-end
+figure through rmq_query_idx_host on page-locked host buffers, the
+reference's own GPU kernels timed on the same inputs, the CPU baseline and
+the SM clocks sampled during the timed region.
+
+The default run adds `sub_records`, each with its own value, ms_per_step,
+roofline, parity sample and clocks:
+  mixture_n2e26  n = q = 2^26, 1 % of entries tied at the minimum, lengths one
+                 third each uniform [1, n], lognormal(2^13, 1), lognormal(2^5,
+                 0.7), t = 64 (the mixed-length target: >= 0.60 of HBM peak)
+  c3_n2e28       n = 2^28 with 1 % ties, q = 2^27, the same mixture, t = 64
+  c1_n2e20       n = 2^20, q = 2^16, lengths uniform [1, n] (the reference's
+                 CPU case), L2 flushed between steps, against the L2 read rate
+  batched_c4     4096 arrays (batched form vs a per-array loop of the plain
+                 kernels with buffers allocated up front)
+  served_c5      the serving loop on a Poisson trace (p50 / p99 latency;
+                 capacity vs a per-request loop of the plain kernel)
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--mode plain|batched|serve] [--n N --q Q --lr L --t T --ties F]
+                  [--mode plain|batched|serve] [--sub-records all|none|a,b]
+                  [--n N --q Q --lr L --t T --ties F]
 
 Under torchrun each rank builds and queries its own replica on its own GPU
 (no collective on the data path); value = all ranks' queries / max-over-ranks
 time ("weak" scaling).  The reference arm (--impl reference) times the
-reference's CPU brute-force scan (restated in oracle/) on the host cores.
+reference's CPU brute-force scan (restated in oracle/, inputs from the
+oracle's own generators) on the host cores.
 """
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import os
 import statistics
@@ -237,7 +254,11 @@ def barrier(ws: int):
 
 
 # ---------------------------------------------------------------------------
+# ---------------------------------------------------------------------------
+# inputs
+# ---------------------------------------------------------------------------
 def make_inputs(n: int, q: int, lr: int, seed: int, ties: float = 0.0):
+    """The GPU arm's inputs, from the library's host generators."""
     import rmq_gb300 as R
     a = R.gen_array(n, seed)
     if ties > 0.0:
@@ -246,44 +267,65 @@ def make_inputs(n: int, q: int, lr: int, seed: int, ties: float = 0.0):
     return a, qs
 
 
+def make_inputs_oracle(n: int, q: int, lr: int, seed: int, ties: float = 0.0):
+    """The reference arm's inputs, from the oracle's own restatement of the
+    same generators (bit-identical to make_inputs; no product library is
+    loaded)."""
+    from oracle import oracle
+    a = oracle.gen_array(n, seed)
+    if ties > 0.0:
+        oracle.plant_min_ties(a, ties, seed)
+    return a, oracle.gen_queries(q, lr, n, seed)
+
+
+def algorithmic_bytes_chunked(qs: np.ndarray, n: int, chunk: int = 1 << 22) -> int:
+    """algorithmic_bytes (min + argmin) over a large query set, in chunks."""
+    return sum(algorithmic_bytes(qs[i:i + chunk], n, True, True) for i in range(0, qs.shape[0], chunk))
+
+
 def cpu_baseline(a: np.ndarray, qs: np.ndarray, budget_s: float, with_idx: bool = True) -> dict:
-    """The reference's brute-force scan (oracle/ restatement of cpu_rmq /
-    cpu_rmq_idx) on all host threads over consecutive chunks of the same
-    query set until `budget_s` of wall time is used."""
+    """The reference's brute-force scan as it runs it (oracle restatement of
+    cpu_rmq / cpu_rmq_idx, src/cpu_methods.h:18-77, one OpenMP parallel for
+    with the default schedule) on all host threads, over consecutive chunks
+    of the same query set until `budget_s` of wall time is used."""
     from oracle import oracle
     threads = oracle.max_threads()
     chunk = 1 << 14
     done = 0
     t0 = time.perf_counter()
     while done < qs.shape[0] and time.perf_counter() - t0 < budget_s:
-        part = qs[done: done + chunk]
-        oracle.rmq_min(a, part, threads)
+        part = np.ascontiguousarray(qs[done: done + chunk])
+        oracle.cpu_rmq(a, part, threads)
         if with_idx:
-            oracle.rmq_argmin(a, part, threads)
+            oracle.cpu_rmq_idx(a, part, threads)
         done += part.shape[0]
     dt = time.perf_counter() - t0
     return {"value": done / dt, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"first {done} of the {qs.shape[0]} queries (min{' + argmin' if with_idx else ''}), "
-                      f"{dt:.1f} s wall on {threads} threads"}
+                      f"{dt:.1f} s wall on {threads} threads",
+            "schedule": "cpu_rmq / cpu_rmq_idx restated with the reference's default OpenMP schedule "
+                        "(src/cpu_methods.h:28, :65)"}
 
 
 def run_reference(args, ws, rank):
-    """Reference arm: the reference's CPU scan (alg 0 + alg 100 semantics) on
-    the host cores, rank 0 only; each step is a bounded sample."""
+    """Reference arm: the reference's CPU scan (alg 0 + alg 100, as
+    cpu_rmq / cpu_rmq_idx run it) on the host cores, rank 0 only; each step is
+    a bounded sample.  Inputs come from the oracle's generators, so no
+    product library is loaded."""
     if rank != 0:
         return
     from oracle import oracle
-    a, qs = make_inputs(args.n, args.q, args.lr, args.seed, args.ties)
+    a, qs = make_inputs_oracle(args.n, args.q, args.lr, args.seed, args.ties)
     threads = oracle.max_threads()
     per_step = args.ref_step_queries
     rng = np.random.default_rng(args.seed)
     times = []
     for i in range(args.warmup + args.steps):
         start = int(rng.integers(0, max(1, qs.shape[0] - per_step)))
-        part = qs[start: start + per_step]
+        part = np.ascontiguousarray(qs[start: start + per_step])
         t0 = time.perf_counter()
-        oracle.rmq_min(a, part, threads)
-        oracle.rmq_argmin(a, part, threads)
+        oracle.cpu_rmq(a, part, threads)
+        oracle.cpu_rmq_idx(a, part, threads)
         dt = time.perf_counter() - t0
         if i >= args.warmup:
             times.append(dt)
@@ -296,7 +338,9 @@ def run_reference(args, ws, rank):
         "config": workload_config(args, "not applicable (host CPU run, a bounded sample of the queries per step)"),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{per_step} consecutive queries per step (random offset), "
-                                   f"min + argmin brute-force scan on {threads} threads"},
+                                   f"min + argmin brute-force scan on {threads} threads",
+                         "schedule": "cpu_rmq / cpu_rmq_idx restated with the reference's default "
+                                     "OpenMP schedule (src/cpu_methods.h:28, :65)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -319,43 +363,85 @@ LENGTH_LAWS = {
 L2_FLUSH_BELOW = 258 << 20
 
 
+def workload_name(n: int, q: int, lr: int, ties: float) -> str:
+    law = LENGTH_LAWS.get(lr, f"len = {lr}" if lr > 0 else f"length law {lr}")
+    tie = f" with {100 * ties:g} % of entries set to the global minimum" if ties > 0 else ""
+    return (f"plain single array: n=2^{np.log2(n):g} fp32 uniform[0,1){tie}, q=2^{np.log2(q):g} queries, "
+            f"{law}, l uniform in [0,n-len]; min + argmin per query")
+
+
 def workload_config(args, l2_note: str = "inputs larger than L2 (no flush)") -> dict:
-    law = LENGTH_LAWS.get(args.lr, f"len = {args.lr}" if args.lr > 0 else f"length law {args.lr}")
-    ties = f" with {100 * args.ties:g} % of entries set to the global minimum" if args.ties > 0 else ""
-    return {"workload": f"plain single array: n=2^{np.log2(args.n):g} fp32 uniform[0,1){ties}, "
-                        f"q=2^{np.log2(args.q):g} queries, {law}, "
-                        f"l uniform in [0,n-len]; min + argmin per query",
+    return {"workload": workload_name(args.n, args.q, args.lr, args.ties),
             "n": args.n, "q": args.q, "lr_code": args.lr, "seed": args.seed, "ties": args.ties,
             "variant": args.variant, "scan_threshold": args.t, "rf_log": args.rf_log, "lanes": args.lanes,
             "l2": l2_note, "parallelism": f"replicas x{dist_env()[0]}"}
 
 
-def run_ours(args, ws, rank, local):
+# ---------------------------------------------------------------------------
+# L2 read rate (measured here; no datasheet figure exists for GB300)
+# ---------------------------------------------------------------------------
+_L2_PEAK = None
+
+
+def l2_peak(dev) -> dict:
+    """Rate at which the SMs read L2-resident 32-byte sectors with the query
+    kernels' load form (rmq_measure_l2_read over a 32 MiB buffer: in address
+    order, and at hashed sector positions), best of 3 runs of 50 passes."""
+    global _L2_PEAK
+    if _L2_PEAK is None:
+        import torch
+        import rmq_gb300 as R
+        buf = torch.ones(1 << 23, dtype=torch.float32, device=dev)  # 32 MiB
+        seq = max(R.measure_l2_read(buf, 50, False) for _ in range(3))
+        rnd = max(R.measure_l2_read(buf, 50, True) for _ in range(3))
+        del buf
+        _L2_PEAK = {"GBps": seq, "random_sectors_GBps": rnd,
+                    "how": "rmq_measure_l2_read: 32 MiB buffer, 256-bit loads with L1 bypassed, 64 warps/SM, "
+                           "best of 3 x 50 passes (sequential sectors = peak; hashed sectors for context)"}
+    return _L2_PEAK
+
+
+# ---------------------------------------------------------------------------
+# plain single-array measurement (headline and sub-records)
+# ---------------------------------------------------------------------------
+def parity_sample(a: np.ndarray, qs: np.ndarray, out_min, out_idx, seed: int, size: int = 1 << 14) -> bool:
+    """The timed outputs on a seeded sample of queries against the oracle's
+    sparse table (checked against the brute-force scan in the CPU tests)."""
+    import rmq_gb300 as R
+    from oracle import oracle
+    samp = R.sample_indices(qs.shape[0], size, seed).astype(np.int64)
+    import torch
+    idx_t = torch.from_numpy(samp).to(out_min.device)
+    got_m = out_min[idx_t].cpu().numpy()
+    got_i = out_idx[idx_t].cpu().numpy().view(np.uint32)
+    exp_m, exp_i = oracle.Sparse(a).query(np.ascontiguousarray(qs[samp]))
+    return bool(got_m.tobytes() == exp_m.tobytes() and np.array_equal(got_i, exp_i))
+
+
+def plain_measure(n, q, lr, ties, t, seed, args, dev, stream, ws, *, tag_suffix="", l2_bound=False,
+                  keep=False):
+    """Builds the hierarchy over a generated array and times `args.steps`
+    launches of the min + argmin query kernel over q generated queries (CUDA
+    events on the launching stream; L2 flushed between steps when the inputs
+    fit in it).  Returns the record and, with keep, the buffers for the
+    headline's extra measurements."""
     import torch
     import rmq_gb300 as R
 
-    torch.cuda.set_device(local)
-    dev = torch.device("cuda", local)
-    dist_init(ws, "nccl")
-
-    a, qs = make_inputs(args.n, args.q, args.lr, args.seed + rank, args.ties)
-    q = qs.shape[0]
+    a, qs = make_inputs(n, q, lr, seed, ties)
     dv = torch.from_numpy(a).to(dev)
     dq = torch.from_numpy(qs.view(np.int32)).to(dev)
     out_min = torch.empty(q, dtype=torch.float32, device=dev)
     out_idx = torch.empty(q, dtype=torch.int32, device=dev)
-    stream = torch.cuda.Stream(device=dev)
     sh = stream.cuda_stream
-
     # The first build also loads the kernels (lazy module loading); the
     # reported build time is that of a second, warm build.
-    R.Hierarchy(dv, variant=args.variant, t=args.t, rf_log=args.rf_log, lanes=args.lanes,
+    R.Hierarchy(dv, variant=args.variant, t=t, rf_log=args.rf_log, lanes=args.lanes,
                 l2_persist=args.l2_persist, stream=stream).close()
-    h = R.Hierarchy(dv, variant=args.variant, t=args.t, rf_log=args.rf_log, lanes=args.lanes,
+    h = R.Hierarchy(dv, variant=args.variant, t=t, rf_log=args.rf_log, lanes=args.lanes,
                     l2_persist=args.l2_persist, stream=stream)
     info = h.info()
     torch.cuda.synchronize()
-
     lr_ptr, idx_ptr, min_ptr = int(dq.data_ptr()), int(out_idx.data_ptr()), int(out_min.data_ptr())
 
     def step():
@@ -363,11 +449,7 @@ def run_ours(args, ws, rank, local):
         if st != 0:
             raise R.RMQError(st, "rmq_query_idx")
 
-    # --- device-resident throughput -------------------------------------------
-    # A workload whose inputs and outputs fit in L2 twice over is timed step by
-    # step with L2 flushed between steps (a 512 MiB write, untimed);
-    # otherwise the steps run back to back (the inputs exceed L2).
-    footprint = 4 * args.n + int(info.level_bytes) + 16 * q
+    footprint = 4 * n + int(info.level_bytes) + 16 * q
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev) if footprint < L2_FLUSH_BELOW else None
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
@@ -376,7 +458,7 @@ def run_ours(args, ws, rank, local):
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * args.steps)]
     barrier(ws)
     torch.cuda.synchronize()
-    with ClockSampler(local) as clocks:
+    with ClockSampler(dev.index) as clocks:
         with torch.cuda.stream(stream):
             for k in range(args.steps):
                 if flush is not None:
@@ -389,13 +471,11 @@ def run_ours(args, ws, rank, local):
     per_launch = [ev[2 * k].elapsed_time(ev[2 * k + 1]) for k in range(args.steps)]
     total_ms = sum(per_launch) if flush is not None else ev[0].elapsed_time(ev[2 * args.steps - 1])
     total_ms = max_over_ranks(total_ms, ws, dev)
-    ms_step = total_ms / args.steps
     value = aggregate_value(q, args.steps, total_ms, ws)
-
     l2_note = ("L2 flushed between steps (512 MiB write, untimed)" if flush is not None
                else "inputs larger than L2 (no flush)")
 
-    # --- minimum-only pass (same kernel family, no argmin), for reference ------
+    # minimum-only pass (same kernel family, no argmin)
     with torch.cuda.stream(stream):
         for _ in range(max(1, args.warmup)):
             h.query_raw(lr_ptr, q, min_ptr, sh)
@@ -410,40 +490,105 @@ def run_ours(args, ws, rank, local):
     min_ms = (sum(em[2 * k].elapsed_time(em[2 * k + 1]) for k in range(args.steps)) if flush is not None
               else em[0].elapsed_time(em[2 * args.steps - 1]))
     min_only_qps = q * args.steps / (min_ms / 1e3)
-
-    # --- end to end: pinned host queries -> device -> host results -------------
-    e2e = run_e2e(args, h, qs, dev, ws, out_idx, out_min, dq)
-
-    # --- parity spot check of the timed outputs (not timed) ---------------------
-    from oracle import oracle
-    samp = R.sample_indices(q, 1 << 12, args.seed).astype(np.int64)
-    got_m = out_min.cpu().numpy()[samp]
-    got_i = out_idx.cpu().numpy().view(np.uint32)[samp]
-    exp_m = oracle.rmq_min(a, qs[samp])
-    exp_i = oracle.rmq_argmin(a, qs[samp])
-    parity = bool(got_m.tobytes() == exp_m.tobytes() and np.array_equal(got_i, exp_i))
+    # restore the argmin + min outputs (the minimum-only pass rewrote out_min)
+    with torch.cuda.stream(stream):
+        step()
+    torch.cuda.synchronize()
+    parity = parity_sample(a, qs, out_min, out_idx, seed)
 
     peaks = measured_peaks()
-    alg_bytes = algorithmic_bytes(qs, args.n, True, True)
     kernel_ms = statistics.mean(per_launch)
+    alg_bytes = algorithmic_bytes_chunked(qs, n)
     achieved = alg_bytes / (kernel_ms / 1e3) / 1e9
     tag = f"vl-rf{1 << info.rf_log}" if info.variant == 2 else f"cl-rf{1 << info.rf_log}-g{info.lanes}"
-    tpq = traffic_per_query(tag)
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                "frac": achieved / peaks["hbm_gbs"],
-                "traffic": (tpq * q) if tpq is not None else None,
-                "peak_source": f"{peaks['source']} (MEASURED_PEAKS.json hbm_gbs, copy burst)",
-                "algorithmic_bytes_per_launch": alg_bytes,
-                "kernel": f"query_{'vl' if info.variant == 2 else 'cl'}_kernel (argmin+min), {tag}",
-                "kernel_ms_mean": kernel_ms}
-    # The coarse levels' bytes (canonical model) go against L2; no L2 peak is
-    # measured here, so the figure is an achieved rate only.
+    tpq = traffic_per_query(tag + tag_suffix)
+    l2p = l2_peak(dev)
     l2_sample = qs[: 1 << 20]
-    l2_per_q = SECTOR * float(coarse_sectors(l2_sample, args.n).mean()) if l2_sample.shape[0] else 0.0
-    roofline["l2"] = {"algorithmic_bytes_per_query": l2_per_q,
-                      "achieved_GBps": l2_per_q * q / (kernel_ms / 1e3) / 1e9,
-                      "peak": None, "sample": f"first {l2_sample.shape[0]} queries",
-                      "model": "32 B x sectors of levels >= 1 read by the canonical descent (rf 32, t 64)"}
+    l2_per_q = SECTOR * float(coarse_sectors(l2_sample, n).mean()) if l2_sample.shape[0] else 0.0
+    l2_achieved = l2_per_q * q / (kernel_ms / 1e3) / 1e9
+    l2 = {"algorithmic_bytes_per_query": l2_per_q, "achieved_GBps": l2_achieved, "peak": l2p["GBps"],
+          "frac": l2_achieved / l2p["GBps"], "peak_random_sectors_GBps": l2p["random_sectors_GBps"],
+          "peak_source": "measured here (" + l2p["how"] + ")",
+          "sample": f"first {l2_sample.shape[0]} queries",
+          "model": "32 B x sectors of levels >= 1 read by the canonical descent (rf 32, t 64)"}
+    kernel = f"query_{'vl' if info.variant == 2 else 'cl'}_kernel (argmin+min), {tag}"
+    if l2_bound:
+        # every input of this workload fits in L2: the same algorithmic bytes
+        # go against the L2 read rate (inputs are flushed from L2 between steps)
+        roofline = {"bound": "l2", "achieved": achieved, "peak": l2p["GBps"], "unit": "GB/s",
+                    "frac": achieved / l2p["GBps"], "traffic": (tpq * q) if tpq is not None else None,
+                    "peak_source": "measured here (" + l2p["how"] + ")",
+                    "algorithmic_bytes_per_launch": alg_bytes, "kernel": kernel, "kernel_ms_mean": kernel_ms,
+                    "hbm_frac": achieved / peaks["hbm_gbs"]}
+    else:
+        roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                    "frac": achieved / peaks["hbm_gbs"], "traffic": (tpq * q) if tpq is not None else None,
+                    "peak_source": f"{peaks['source']} (MEASURED_PEAKS.json hbm_gbs, copy burst)",
+                    "algorithmic_bytes_per_launch": alg_bytes, "kernel": kernel, "kernel_ms_mean": kernel_ms,
+                    "l2": l2}
+    build_bytes = 4 * n + 8 * sum(info.sizes()[1:])
+    rec = {"value": value, "unit": UNIT, "ms_per_step": total_ms / args.steps, "steps": args.steps,
+           "warmup": args.warmup, "workload": workload_name(n, q, lr, ties),
+           "n": n, "q": q, "lr_code": lr, "ties": ties, "seed": seed, "scan_threshold": t, "l2": l2_note,
+           "roofline": roofline, "clocks": clocks.summary(), "parity_sample_ok": parity,
+           "parity_sample": "2^14 seeded queries of the timed outputs vs the oracle's sparse table",
+           "min_only_queries_per_s": min_only_qps, "gpu_launches": args.steps,
+           "hierarchy": {"variant": ["auto", "cl", "vl"][info.variant], "rf": 1 << info.rf_log,
+                         "t": int(info.scan_threshold), "levels": int(info.num_levels),
+                         "lanes": int(info.lanes), "level_bytes": int(info.level_bytes),
+                         "build_ms": float(info.build_ms),
+                         "build_GBps": build_bytes / (float(info.build_ms) / 1e3) / 1e9
+                         if info.build_ms > 0 else None}}
+    ctx = None
+    if keep:
+        ctx = {"a": a, "qs": qs, "dv": dv, "dq": dq, "h": h, "out_min": out_min, "out_idx": out_idx,
+               "min_only_qps": min_only_qps, "clocks": clocks, "per_launch": per_launch,
+               "total_ms": total_ms, "l2_note": l2_note}
+    else:
+        h.close()
+        del dv, dq, out_min, out_idx, flush
+        gc.collect()
+        torch.cuda.empty_cache()
+    return rec, ctx
+
+
+PLAIN_SUBS = {
+    "mixture_n2e26": {"n": 1 << 26, "q": 1 << 26, "lr": -8, "ties": 0.01, "t": 64, "tag": "-mixture",
+                      "target": {"what": "plain kernel at n = 2^26 with mixed query lengths: "
+                                         "roofline.frac >= 0.60 of the HBM peak", "frac_at_least": 0.60}},
+    "c3_n2e28": {"n": 1 << 28, "q": 1 << 27, "lr": -8, "ties": 0.01, "t": 64, "tag": "-n2e28"},
+    "c1_n2e20": {"n": 1 << 20, "q": 1 << 16, "lr": -1, "ties": 0.0, "t": 64, "tag": "-n2e20", "l2": True},
+}
+SUB_RECORDS = list(PLAIN_SUBS) + ["batched_c4", "served_c5"]
+
+
+def selected_sub_records(spec: str) -> list[str]:
+    if spec in ("", "none"):
+        return []
+    if spec == "all":
+        return list(SUB_RECORDS)
+    names = [x.strip() for x in spec.split(",") if x.strip()]
+    bad = [x for x in names if x not in SUB_RECORDS]
+    if bad:
+        raise SystemExit(f"bench.py: unknown sub-records {bad}; choose from {SUB_RECORDS}")
+    return names
+
+
+def run_ours(args, ws, rank, local):
+    import torch
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    dist_init(ws, "nccl")
+    stream = torch.cuda.Stream(device=dev)
+
+    rec, ctx = plain_measure(args.n, args.q, args.lr, args.ties, args.t, args.seed + rank, args, dev, stream, ws,
+                             keep=True)
+    a, qs, h = ctx["a"], ctx["qs"], ctx["h"]
+    q = qs.shape[0]
+
+    # --- end to end: pinned host queries -> device -> host results -------------
+    e2e = run_e2e(args, h, qs, dev, ws, ctx["out_idx"], ctx["out_min"], ctx["dq"])
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -461,48 +606,159 @@ def run_ours(args, ws, rank, local):
             reference_gpu = {"unavailable": "n % 4 != 0 (the reference VL kernel reads whole float4s)"}
         else:
             reference_gpu = {}
-            ours_min = out_min.clone()
+            ours_min = ctx["out_min"].clone()
             for variant, t in (("cl", 64), ("vl", 32), ("cl", args.t), ("vl", args.t)):
                 key = f"{variant}_t{t}"
                 if key in reference_gpu:
                     continue
                 with torch.cuda.stream(stream):
-                    qps, ref_out = ref_gpu.time_reference(dv, dq, variant, t, steps=args.steps, warmup=3)
+                    qps, ref_out = ref_gpu.time_reference(ctx["dv"], ctx["dq"], variant, t, steps=args.steps,
+                                                          warmup=3)
                 reference_gpu[key] = {"queries_per_s": qps,
                                       "minima_equal_ours": bool(torch.equal(ref_out.view(torch.int32),
                                                                             ours_min.view(torch.int32)))}
                 del ref_out
             best = max(v["queries_per_s"] for v in reference_gpu.values())
             reference_gpu["best_queries_per_s"] = best
-            reference_gpu["ours_min_only_vs_best"] = min_only_qps / best
-            reference_gpu["ours_min_argmin_vs_best"] = value / ws / best
+            reference_gpu["ours_min_only_vs_best"] = ctx["min_only_qps"] / best
+            reference_gpu["ours_min_argmin_vs_best"] = rec["value"] / ws / best
 
-    build_bytes = 4 * args.n + 8 * sum(info.sizes()[1:])
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "metric": METRIC, "value": rec["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": rec["ms_per_step"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generators; no public dataset)",
-        "config": workload_config(args, l2_note),
-        "roofline": roofline,
+        "config": workload_config(args, ctx["l2_note"]),
+        "roofline": rec["roofline"],
         "cpu_baseline": cpu,
         "e2e": e2e,
-        "clocks": clocks.summary(),
+        "clocks": rec["clocks"],
         "gpu_launches": args.steps,
-        "parity_sample_ok": parity,
-        "min_only_queries_per_s": min_only_qps,
+        "parity_sample_ok": rec["parity_sample_ok"],
+        "min_only_queries_per_s": rec["min_only_queries_per_s"],
         "reference_gpu": reference_gpu,
-        "hierarchy": {"variant": ["auto", "cl", "vl"][info.variant], "rf": 1 << info.rf_log,
-                      "t": int(info.scan_threshold), "levels": int(info.num_levels),
-                      "lanes": int(info.lanes), "level_bytes": int(info.level_bytes),
-                      "build_ms": float(info.build_ms),
-                      "build_GBps": build_bytes / (float(info.build_ms) / 1e3) / 1e9 if info.build_ms > 0 else None},
+        "hierarchy": rec["hierarchy"],
     }
     h.close()
+    del ctx
+    gc.collect()
+    torch.cuda.empty_cache()
+
+    subs = {}
+    for name in selected_sub_records(args.sub_records):
+        t0 = time.perf_counter()
+        try:
+            if name in PLAIN_SUBS:
+                c = PLAIN_SUBS[name]
+                r, _ = plain_measure(c["n"], c["q"], c["lr"], c["ties"], c["t"], args.seed + rank, args, dev,
+                                     stream, ws, tag_suffix=c["tag"], l2_bound=c.get("l2", False))
+                if "target" in c:
+                    r["target"] = dict(c["target"], met=bool(r["roofline"]["frac"] >= c["target"]["frac_at_least"]))
+            elif name == "batched_c4":
+                r = batched_record(args, ws, rank, dev)
+            else:
+                r = served_record(args, ws, rank, dev)
+        except Exception as exc:  # a failed sub-record is reported, the headline stands
+            r = {"error": f"{type(exc).__name__}: {exc}"}
+        r["wall_s"] = time.perf_counter() - t0
+        subs[name] = r
+        gc.collect()
+        torch.cuda.empty_cache()
+    if subs:
+        line["sub_records"] = subs
+        line["targets"] = targets_summary(subs)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def targets_summary(subs: dict) -> dict:
+    """The benchmark spec's targets next to the measured figures."""
+    out = {}
+    m = subs.get("mixture_n2e26", {})
+    if "roofline" in m:
+        out["plain_mixture_n2e26_frac"] = {"value": m["roofline"]["frac"], "target": 0.60,
+                                          "met": m["roofline"]["frac"] >= 0.60}
+    b = subs.get("batched_c4", {})
+    if "speedup_vs_plain_loop" in b:
+        out["batched_vs_per_array_plain_loop"] = {"value": b["speedup_vs_plain_loop"], "target": 3.0,
+                                                  "met": b["speedup_vs_plain_loop"] >= 3.0,
+                                                  "loop": b["loop_plain_kernels"]["what"]}
+    s = subs.get("served_c5", {})
+    if "speedup_capacity_vs_loop" in s:
+        out["served_capacity_vs_per_request_loop"] = {"value": s["speedup_capacity_vs_loop"], "target": 3.0,
+                                                      "met": s["speedup_capacity_vs_loop"] >= 3.0,
+                                                      "loop": s["loop_plain_kernel"]["what"]}
+    return out
+
+
+# ---------------------------------------------------------------------------
+# host memory placement for the end-to-end figure
+# ---------------------------------------------------------------------------
+def _read(path: str) -> str | None:
+    try:
+        return Path(path).read_text().strip()
+    except OSError:
+        return None
+
+
+def _cpulist(text: str) -> set[int]:
+    cpus = set()
+    for part in text.split(","):
+        part = part.strip()
+        if not part:
+            continue
+        if "-" in part:
+            a, b = part.split("-")
+            cpus.update(range(int(a), int(b) + 1))
+        else:
+            cpus.add(int(part))
+    return cpus
+
+
+def gpu_host_node(gpu_index: int) -> dict:
+    """The host NUMA node the GPU's PCI function reports (sysfs), and that
+    node's CPUs."""
+    out = {"gpu_pci_bus_id": None, "gpu_numa_node": None, "node_cpus": None}
+    try:
+        bus = subprocess.run(["nvidia-smi", "-i", str(gpu_index), "--query-gpu=pci.bus_id",
+                              "--format=csv,noheader"], capture_output=True, text=True, timeout=20).stdout.strip()
+    except (OSError, subprocess.TimeoutExpired):
+        return out
+    if not bus:
+        return out
+    # nvidia-smi prints an 8-digit domain ("00000009:01:00.0"); sysfs uses 4
+    dom, rest = bus.split(":", 1)
+    sysfs = f"{int(dom, 16):04x}:{rest}".lower()
+    out["gpu_pci_bus_id"] = sysfs
+    node = _read(f"/sys/bus/pci/devices/{sysfs}/numa_node")
+    if node is not None and node.lstrip("-").isdigit():
+        out["gpu_numa_node"] = int(node)
+        if int(node) >= 0:
+            cpus = _read(f"/sys/devices/system/node/node{int(node)}/cpulist")
+            if cpus:
+                out["node_cpus"] = sorted(_cpulist(cpus))
+    return out
+
+
+def buffer_nodes(addr: int) -> dict:
+    """Pages per NUMA node of the mapping holding host address `addr`
+    (/proc/self/numa_maps)."""
+    maps = _read("/proc/self/maps") or ""
+    start = None
+    for line in maps.splitlines():
+        lo, hi = (int(x, 16) for x in line.split()[0].split("-"))
+        if lo <= addr < hi:
+            start = lo
+            break
+    if start is None:
+        return {}
+    for line in (_read("/proc/self/numa_maps") or "").splitlines():
+        fields = line.split()
+        if fields and int(fields[0], 16) == start:
+            return {f.split("=")[0]: int(f.split("=")[1]) for f in fields if f[:1] == "N" and "=" in f}
+    return {}
 
 
 def run_e2e(args, h, qs, dev, ws, out_idx, out_min, d_q) -> dict:
@@ -513,9 +769,26 @@ def run_e2e(args, h, qs, dev, ws, out_idx, out_min, d_q) -> dict:
     must equal those of the device-buffer call."""
     import torch
     q = qs.shape[0]
+    # Page-locked buffers on the GPU's host node: the thread is bound to that
+    # node's CPUs while it allocates (first touch places the pages there) and
+    # while it runs the end-to-end steps; the placement is recorded.
+    place = gpu_host_node(dev.index)
+    prev_aff = os.sched_getaffinity(0) if hasattr(os, "sched_getaffinity") else None
+    bound = False
+    if prev_aff is not None and place["node_cpus"]:
+        local = set(place["node_cpus"]) & prev_aff
+        if local:
+            os.sched_setaffinity(0, local)
+            bound = True
     h_q = torch.from_numpy(qs.view(np.int32).reshape(-1)).pin_memory()
     h_min = torch.empty(q, dtype=torch.float32).pin_memory()
     h_idx = torch.empty(q, dtype=torch.int32).pin_memory()
+    h_min.fill_(0.0)
+    h_idx.fill_(0)
+    place["thread_bound_to_node_cpus"] = bound
+    place["buffer_pages_by_node"] = {"queries": buffer_nodes(int(h_q.data_ptr())),
+                                     "argmin": buffer_nodes(int(h_idx.data_ptr())),
+                                     "min": buffer_nodes(int(h_min.data_ptr()))}
 
     def one_pass():
         st = h.query_idx_host_raw(int(h_q.data_ptr()), q, int(h_idx.data_ptr()), int(h_min.data_ptr()))
@@ -537,6 +810,9 @@ def run_e2e(args, h, qs, dev, ws, out_idx, out_min, d_q) -> dict:
     link["achieved_GBps"] = 16 * q / step_s / 1e9
     link["frac_of_duplex"] = link["achieved_GBps"] / link["duplex_GBps"]
     link["kernel_ms_by_buffer_placement"] = placement_breakdown(h, q, d_q, out_idx, out_min, h_q, h_idx, h_min)
+    link["numa"] = place
+    if bound:
+        os.sched_setaffinity(0, prev_aff)
     return {"value": ws * q * args.steps / dt, "unit": UNIT, "h2d_bytes_per_step": 8 * q,
             "d2h_bytes_per_step": 8 * q,
             "api": "rmq_query_idx_host on page-locked host buffers (kernel reads / writes host memory)",
@@ -618,19 +894,23 @@ def host_link_rates(h_q, h_idx, h_min, d_idx, d_min, reps: int = 3) -> dict:
     return out
 
 
-def run_batched(args, ws, rank, local):
+# ---------------------------------------------------------------------------
+# batched form (4096 arrays)
+# ---------------------------------------------------------------------------
+def batched_record(args, ws, rank, dev) -> dict:
     """Batched workload: 4096 arrays, sizes log-uniform in [2^10, 2^22],
     uniform [0, 1) values, min(4 x size, 2^20) queries per array with lengths
     lognormal(median sqrt(size), sigma 1) clamped to [1, size].  One step =
     build of every array + every query (one CUDA graph launch), inputs
-    resident.  Compared with per-array loops of the plain kernel."""
+    resident.  Compared with the per-array loop of the plain kernels over the
+    same preallocated buffers (rmq_batch_run_per_array: per array the
+    single-array build and query launches, one stream, no synchronisation),
+    and with a per-array loop through the public API (rmq_build, which
+    allocates and waits, + rmq_query_idx)."""
     import torch
     import rmq_gb300 as R
     from oracle import oracle
 
-    torch.cuda.set_device(local)
-    dev = torch.device("cuda", local)
-    dist_init(ws, "nccl")
     rng = np.random.default_rng(args.seed + rank)
     A = args.batch_arrays
     sizes = np.exp(rng.uniform(np.log(2.0 ** 10), np.log(2.0 ** 22), A)).astype(np.uint64)
@@ -660,7 +940,7 @@ def run_batched(args, ws, rank, local):
     torch.cuda.synchronize()
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
     barrier(ws)
-    with ClockSampler(local) as clocks:
+    with ClockSampler(dev.index) as clocks:
         ev[0].record(stream)
         for _ in range(args.steps):
             b.run(stream=stream)
@@ -688,7 +968,27 @@ def run_batched(args, ws, rank, local):
         parity &= out_min[s0:s1].cpu().numpy().tobytes() == oracle.rmq_min(x, qh).tobytes()
         parity &= np.array_equal(out_idx[s0:s1].cpu().numpy().view(np.uint32), oracle.rmq_argmin(x, qh))
 
-    # per-array loops of the plain kernel (rmq_build + rmq_query_idx per array)
+    # comparator: the per-array loop of the plain kernels (C side, buffers
+    # allocated up front, one stream, no synchronisation between arrays)
+    ref_min, ref_idx = out_min.clone(), out_idx.clone()
+    out_min.fill_(-1.0)
+    out_idx.fill_(-1)
+    loop_steps = max(1, min(args.steps, 5))
+    with torch.cuda.stream(stream):
+        b.run_per_array(stream=stream)
+    torch.cuda.synchronize()
+    loop_same = bool(torch.equal(out_idx, ref_idx) and torch.equal(out_min.view(torch.int32),
+                                                                   ref_min.view(torch.int32)))
+    e0.record(stream)
+    for _ in range(loop_steps):
+        b.run_per_array(stream=stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    loop_ms = e0.elapsed_time(e1) / loop_steps
+    loop_value = Q / (loop_ms / 1e3)
+    del ref_min, ref_idx
+
+    # a per-array loop through the public API (allocating rmq_build + query)
     hs = []
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -701,38 +1001,47 @@ def run_batched(args, ws, rank, local):
         hs.append(h)
     torch.cuda.synchronize()
     loop_api_s = time.perf_counter() - t0
-    e0.record(stream)
-    for a in range(A):
-        s0, s1 = int(qo[a]), int(qo[a + 1])
-        hs[a].query_idx_raw(int(lr[s0:s1].data_ptr()), s1 - s0, int(out_idx[s0:s1].data_ptr()),
-                            int(out_min[s0:s1].data_ptr()), stream)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    loop_query_ms = e0.elapsed_time(e1)
     for h in hs:
         h.close()
     b.close()
+    del values, lr, out_min, out_idx
 
-    line = {
+    return {
         "metric": "RMQ queries/s (batched: build + queries of every array per step)", "value": value,
-        "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic (device counter-based generators)",
-        "config": {"workload": f"batched: {A} arrays, sizes log-uniform [2^10, 2^22], "
-                               "queries min(4 size, 2^20) lognormal(sqrt(size), 1.0); min + argmin",
-                   "arrays": A, "total_values": total, "total_queries": Q, "seed": args.seed,
-                   "l2": "inputs larger than L2 (no flush)"},
+        "unit": UNIT, "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+        "workload": f"batched: {A} arrays, sizes log-uniform [2^10, 2^22], "
+                    "queries min(4 size, 2^20) lognormal(sqrt(size), 1.0); min + argmin",
+        "arrays": A, "total_values": total, "total_queries": Q, "seed": args.seed,
+        "l2": "inputs larger than L2 (no flush)", "data": "synthetic (device counter-based generators)",
         "autotuned": {"scan_threshold": int(tuned.scan_threshold), "query_block": int(tuned.query_block),
                       "query_ms": float(tuned.query_ms)},
         "build_ms": build_ms, "query_ms": query_ms,
+        "loop_plain_kernels": {"value": loop_value, "ms_per_step": loop_ms, "steps": loop_steps,
+                               "results_equal_batched": loop_same,
+                               "what": "rmq_batch_run_per_array: per array the plain single-array build and "
+                                       "query launches over the batch's preallocated buffers, one stream, "
+                                       "no synchronisation (C side)"},
         "loop_public_api": {"value": Q / loop_api_s, "seconds": loop_api_s,
-                            "what": "per array: rmq_build (alloc + build + sync) + rmq_query_idx"},
-        "loop_prebuilt_queries": {"value": Q / (loop_query_ms / 1e3), "ms": loop_query_ms,
-                                  "what": "per array: rmq_query_idx launch on a prebuilt handle"},
+                            "what": "per array from Python: rmq_build (allocates, builds, waits) + rmq_query_idx"},
+        "speedup_vs_plain_loop": value / loop_value,
         "speedup_vs_loop_public_api": value / (Q / loop_api_s),
-        "speedup_vs_loop_prebuilt_queries": (Q / (query_ms / 1e3)) / (Q / (loop_query_ms / 1e3)),
         "clocks": clocks.summary(), "gpu_launches": 3 * args.steps, "parity_sample_ok": bool(parity),
     }
+
+
+def run_batched(args, ws, rank, local):
+    import torch
+    torch.cuda.set_device(local)
+    dist_init(ws, "nccl")
+    rec = batched_record(args, ws, rank, torch.device("cuda", local))
+    line = {"metric": rec.pop("metric"), "value": rec.pop("value"), "unit": rec.pop("unit"), "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": rec.pop("ms_per_step"),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": rec.pop("data"), "config": {"workload": rec.pop("workload"), "arrays": rec["arrays"],
+                                                "total_values": rec["total_values"],
+                                                "total_queries": rec["total_queries"], "seed": args.seed,
+                                                "l2": rec.pop("l2")}}
+    line.update(rec)
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -778,19 +1087,21 @@ def serve_trace(rng, sizes, seconds, rate, reg_frac, seed):
     return ev, lr, n_of
 
 
-def run_serve(args, ws, rank, local):
+# ---------------------------------------------------------------------------
+# served form
+# ---------------------------------------------------------------------------
+def served_record(args, ws, rank, dev) -> dict:
     """Serving workload: 256 resident arrays (sizes log-uniform [2^16, 2^26],
     device-generated values), a Poisson stream of 20k requests/s for
     --serve-seconds, 5 % of them registering a new array, 64 GiB HBM budget
-    with LRU eviction; p50/p99 request latency and queries/s, plus the same
-    requests issued at once (capacity) against a per-request loop of the
-    plain kernel through the public API."""
+    with LRU eviction; p50/p99 request latency and queries/s.  Capacity: the
+    same requests on the initial arrays issued at once, against the C-side
+    per-request loop of the plain kernel (rmq_serve_serial_loop: per request
+    rmq_query_idx_host on a prebuilt handle, waited for before the next)."""
     import torch
     import rmq_gb300 as R
     from oracle import oracle
 
-    torch.cuda.set_device(local)
-    dev = torch.device("cuda", local)
     rng = np.random.default_rng(args.seed + rank)
     sizes = [int(np.exp(rng.uniform(np.log(2.0 ** 16), np.log(2.0 ** 26)))) for _ in range(256)]
     seed_of = lambda a: args.seed * 1000003 + a  # noqa: E731  (the trace uses the same rule)
@@ -798,11 +1109,9 @@ def run_serve(args, ws, rank, local):
     req = ev["kind"] == 0
     Q = int(ev["q"][req].sum())
     # Result buffers written once up front: the replay then measures the
-    # server, not the first-touch page faults of 1.7 GB of fresh host memory.
-    out_i = np.zeros(Q, dtype=np.uint32)
-    out_m = np.zeros(Q, dtype=np.float32)
-    out_i.fill(1)
-    out_m.fill(1.0)
+    # server, not the first-touch page faults of fresh host memory.
+    out_i = np.ones(Q, dtype=np.uint32)
+    out_m = np.ones(Q, dtype=np.float32)
 
     # Warm-up on a throwaway server (a 0.2 s trace over 32 small arrays): the
     # first serving run of a process otherwise carries a cold tail (first
@@ -824,7 +1133,7 @@ def run_serve(args, ws, rank, local):
     wi, wm = np.empty(1, np.uint32), np.empty(1, np.float32)
     for a in range(len(sizes)):
         srv.wait(srv.submit(a, warm, wi, wm))  # every initial array built
-    with ClockSampler(local) as clocks:
+    with ClockSampler(dev.index) as clocks:
         lat, wall = srv.replay(ev, lr, out_i, out_m)
     st = srv.stats()
     lat_req = lat[req & (lat >= 0)]
@@ -847,8 +1156,10 @@ def run_serve(args, ws, rank, local):
     _, cap_wall = srv.replay(cap_ev, lr, out_i, out_m)
     srv.close()
 
-    # per-request loop of the plain kernel through the public API (pinned host
-    # buffers, copy in, rmq_query_idx, copy out, synchronise)
+    # the comparator: a C-side per-request loop of the plain kernel on
+    # prebuilt handles, with page-locked host buffers (rmq_query_idx_host's
+    # direct path: one launch per request, queries read from and results
+    # written to host memory, waited for before the next request)
     vals, hs = [], []
     stream = torch.cuda.Stream(device=dev)
     for a, n in enumerate(sizes):
@@ -859,45 +1170,54 @@ def run_serve(args, ws, rank, local):
     h_lr = torch.from_numpy(lr.view(np.int32).reshape(-1)).pin_memory()
     h_i = torch.empty(Q, dtype=torch.int32).pin_memory()
     h_m = torch.empty(Q, dtype=torch.float32).pin_memory()
-    qmax = int(cap_ev["q"].max())
-    d_lr = torch.empty(2 * qmax, dtype=torch.int32, device=dev)
-    d_i = torch.empty(qmax, dtype=torch.int32, device=dev)
-    d_m = torch.empty(qmax, dtype=torch.float32, device=dev)
+    h_i.fill_(1)
+    h_m.fill_(1.0)
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    with torch.cuda.stream(stream):
-        for e in cap_ev:
-            o, q, aid = int(e["q_offset"]), int(e["q"]), int(e["array_id"])
-            d_lr[: 2 * q].copy_(h_lr[2 * o: 2 * (o + q)], non_blocking=True)
-            hs[aid].query_idx_raw(int(d_lr.data_ptr()), q, int(d_i.data_ptr()), int(d_m.data_ptr()), stream)
-            h_i[o:o + q].copy_(d_i[:q], non_blocking=True)
-            h_m[o:o + q].copy_(d_m[:q], non_blocking=True)
-            stream.synchronize()
-    loop_s = time.perf_counter() - t0
+    R.serve_serial_loop(hs, cap_ev[:64], h_lr, h_i, h_m)  # warm-up
+    loop_s = R.serve_serial_loop(hs, cap_ev, h_lr, h_i, h_m)
+    loop_same = True
+    for e in cap_ev[:: max(1, cap_ev.size // 64)]:
+        o, q = int(e["q_offset"]), int(e["q"])
+        loop_same &= bool(np.array_equal(h_i[o:o + q].numpy().view(np.uint32), out_i[o:o + q]))
     for h in hs:
         h.close()
+    del vals, h_lr, h_i, h_m
 
-    line = {
+    return {
         "metric": "RMQ queries/s (served: continuous batching)", "value": Q / wall, "unit": UNIT,
-        "n_gpus": ws, "steps": 1, "warmup": 1, "ms_per_step": wall * 1e3, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Poisson trace)",
-        "config": {"workload": "serving: 256 resident arrays log-uniform [2^16, 2^26], Poisson 20k req/s, "
-                               "1..2^16 queries per request (log-uniform), lognormal(2^13, 1) lengths, "
-                               "5 % registrations, 64 GiB budget, LRU eviction",
-                   "seconds": args.serve_seconds, "events": int(ev.size), "requests": int(req.sum()),
-                   "queries": Q, "slots": args.serve_slots, "seed": args.seed,
-                   "query_threads": args.serve_threads or "library default"},
+        "steps": 1, "warmup": 1, "ms_per_step": wall * 1e3,
+        "workload": "serving: 256 resident arrays log-uniform [2^16, 2^26], Poisson 20k req/s, "
+                    "1..2^16 queries per request (log-uniform), lognormal(2^13, 1) lengths, "
+                    "5 % registrations, 64 GiB budget, LRU eviction",
+        "data": "synthetic (seeded Poisson trace)",
+        "seconds": args.serve_seconds, "events": int(ev.size), "requests": int(req.sum()),
+        "queries": Q, "slots": args.serve_slots, "seed": args.seed,
+        "query_threads": args.serve_threads or "library default",
         "latency_us": {"p50": float(np.percentile(lat_req, 50)), "p99": float(np.percentile(lat_req, 99)),
                        "mean": float(lat_req.mean()), "max": float(lat_req.max())},
         "offered_queries_per_s": Q / float(ev["t_arrival_s"][-1]),
         "server_stats": st,
         "capacity": {"value": cap_q / cap_wall, "requests": int(cap_ev.size), "queries": cap_q,
                      "what": "same requests on the initial arrays, all arriving at once"},
-        "loop_public_api": {"value": cap_q / loop_s, "seconds": loop_s,
-                            "what": "per request: H2D queries, rmq_query_idx, D2H results, sync (Python loop)"},
+        "loop_plain_kernel": {"value": cap_q / loop_s, "seconds": loop_s, "results_equal_served": loop_same,
+                              "what": "rmq_serve_serial_loop (C side): per request rmq_query_idx_host on a "
+                                      "prebuilt handle, page-locked buffers, waited for before the next"},
         "speedup_capacity_vs_loop": (cap_q / cap_wall) / (cap_q / loop_s),
         "clocks": clocks.summary(), "parity_sample_ok": bool(parity),
     }
+
+
+def run_serve(args, ws, rank, local):
+    import torch
+    torch.cuda.set_device(local)
+    rec = served_record(args, ws, rank, torch.device("cuda", local))
+    line = {"metric": rec.pop("metric"), "value": rec.pop("value"), "unit": rec.pop("unit"), "n_gpus": ws,
+            "steps": 1, "warmup": 1, "ms_per_step": rec.pop("ms_per_step"), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": rec.pop("data"),
+            "config": {"workload": rec.pop("workload"), "seconds": rec["seconds"], "events": rec["events"],
+                       "requests": rec["requests"], "queries": rec["queries"], "slots": rec["slots"],
+                       "seed": args.seed, "query_threads": rec["query_threads"]}}
+    line.update(rec)
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -911,6 +1231,9 @@ def parse_args(argv=None):
     ap.add_argument("--mode", choices=["plain", "batched", "serve"], default="plain",
                     help="plain = the single-array workload (default); batched = 4096 arrays; "
                          "serve = the request-serving loop")
+    ap.add_argument("--sub-records", dest="sub_records", default="all",
+                    help="plain mode: sub-records after the headline: all (default), none, or a comma list of "
+                         + ", ".join(SUB_RECORDS))
     ap.add_argument("--serve-seconds", dest="serve_seconds", type=float, default=2.0)
     ap.add_argument("--serve-slots", dest="serve_slots", type=int, default=4)
     ap.add_argument("--serve-threads", dest="serve_threads", type=int, default=0,

@@ -198,6 +198,7 @@ struct rmq_batch {
     uint32_t* d_argmin = nullptr;
     float* d_min = nullptr;
     bool queries_set = false;
+    std::vector<ArrayDesc> h_descs;  // host copy of the descriptors (per-array loop)
     // graph + timing
     cudaStream_t cap_stream = nullptr;
     cudaGraphExec_t graph = nullptr;
@@ -259,8 +260,9 @@ int plan(rmq_batch* b, uint64_t t, cudaStream_t s) {
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(b->d_tile_off, tile_off.data(), sizeof(uint64_t) * (b->num_arrays + 1),
                             cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);  // host vectors die here
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);  // tile_off dies here; descs are kept
     if (e != cudaSuccess) return status_of(e);
+    b->h_descs.swap(descs);
     b->t = t;
     b->lvl_used = base;
     b->max_levels = max_levels;
@@ -463,6 +465,42 @@ int rmq_batch_run(rmq_batch* b, rmq_stream_t stream) {
         }
     }
     return status_of(cudaGraphLaunch(b->graph, s));
+}
+
+int rmq_batch_run_per_array(rmq_batch* b, rmq_stream_t stream) {
+    rmq::NvtxRange nvtx_range("rmq_batch_run_per_array");
+    if (b == nullptr || !b->queries_set) return RMQ_ERR_ARG;
+    DeviceGuard guard(b->device);
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    for (uint32_t a = 0; a < b->num_arrays; ++a) {
+        const ArrayDesc& d = b->h_descs[a];
+        const rmq::Layout lay = rmq::plan_layout(b->sizes[a], b->t, 3);
+        const float* vals = b->d_values + d.val_off;
+        float* lvl = b->lvl_val + d.lvl_base;
+        uint32_t* idx = b->lvl_idx != nullptr ? b->lvl_idx + d.idx_base : nullptr;
+        cudaError_t e = rmq::launch_build(lay, vals, lvl, idx, s);
+        if (e != cudaSuccess) return status_of(e);
+        const uint64_t q0 = b->q_off[a], q = b->q_off[a + 1] - q0;
+        if (q == 0) continue;
+        rmq::QueryArgs qa;
+        std::memset(&qa, 0, sizeof(qa));
+        for (uint32_t k = 0; k < lay.num_levels; ++k) {
+            qa.lv.val[k] = k == 0 ? vals : lvl + lay.offset[k];
+            qa.lv.idx[k] = (k == 0 || idx == nullptr) ? nullptr : idx + lay.offset[k];
+            qa.lv.size[k] = uint32_t(lay.size[k]);
+        }
+        qa.lv.num_levels = lay.num_levels;
+        qa.qs = reinterpret_cast<const uint2*>(b->d_lr) + q0;
+        qa.q = q;
+        qa.out_min = b->d_min != nullptr ? b->d_min + q0 : nullptr;
+        qa.out_idx = b->d_argmin != nullptr ? b->d_argmin + q0 : nullptr;
+        qa.variant = RMQ_VARIANT_VL;
+        qa.lanes = 8;
+        qa.rf_log = 3;
+        e = rmq::launch_query(qa, s);
+        if (e != cudaSuccess) return status_of(e);
+    }
+    return RMQ_OK;
 }
 
 int rmq_batch_autotune(rmq_batch* b, rmq_stream_t stream, rmq_batch_info* info) {

@@ -131,6 +131,9 @@ def lib() -> ctypes.CDLL:
         L.rmq_debug_bounds_violations.restype = ctypes.c_int
         L.rmq_plan_layout.argtypes = [_U64, _U64, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(RMQInfo)]
         L.rmq_plan_layout.restype = ctypes.c_int
+        L.rmq_measure_l2_read.argtypes = [_P, _U64, ctypes.c_uint32, ctypes.c_int32, _P,
+                                          ctypes.POINTER(ctypes.c_float)]
+        L.rmq_measure_l2_read.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -181,6 +184,18 @@ def plan_layout(n: int, t: int = 0, rf_log: int = 0, variant: str | int = "auto"
     if st != RMQ_OK:
         raise RMQError(st, "rmq_plan_layout")
     return info
+
+
+def measure_l2_read(buf, passes: int = 20, random: bool = False, stream=None) -> float:
+    """L2-resident sector read rate in GB/s over a CUDA float32 tensor (its
+    byte size / 32 a power of two; values >= -1) that fits in L2."""
+    ms = ctypes.c_float()
+    nbytes = buf.numel() * 4
+    st = lib().rmq_measure_l2_read(_dev_ptr(buf), nbytes, passes, 1 if random else 0,
+                                   _stream_handle(stream), ctypes.byref(ms))
+    if st != RMQ_OK:
+        raise RMQError(st, "rmq_measure_l2_read")
+    return nbytes * passes / (ms.value / 1e3) / 1e9
 
 
 def _stream_handle(stream) -> int:
@@ -399,7 +414,7 @@ def _bind_batch() -> ctypes.CDLL:
         L.rmq_batch_create.argtypes = [_P, _P, _P, ctypes.c_uint32, ctypes.POINTER(RMQConfig), _P,
                                        ctypes.POINTER(_P)]
         L.rmq_batch_set_queries.argtypes = [_P, _P, _P, _P, _P, _P]
-        for name in ("rmq_batch_build", "rmq_batch_query", "rmq_batch_run"):
+        for name in ("rmq_batch_build", "rmq_batch_query", "rmq_batch_run", "rmq_batch_run_per_array"):
             getattr(L, name).argtypes = [_P, _P]
         L.rmq_batch_autotune.argtypes = [_P, _P, ctypes.POINTER(BatchInfo)]
         L.rmq_batch_get_info.argtypes = [_P, ctypes.POINTER(BatchInfo)]
@@ -456,6 +471,11 @@ class Batch:
 
     def run(self, stream=None):
         self._call("rmq_batch_run", stream)
+
+    def run_per_array(self, stream=None):
+        """The per-array loop of the plain kernels over the batch's buffers
+        (the batched form's comparator; same results)."""
+        self._call("rmq_batch_run_per_array", stream)
 
     def set_tuning(self, t: int, query_block: int, stream=None) -> None:
         """Applies a known (t, CTA size); rebuild before querying."""
@@ -596,6 +616,8 @@ def _bind_server() -> ctypes.CDLL:
         L.rmq_server_drain.argtypes = [_P, ctypes.c_int64]
         L.rmq_server_replay.argtypes = [_P, _P, _U64, _P, _P, _P, _P, ctypes.POINTER(ctypes.c_double)]
         L.rmq_server_get_stats.argtypes = [_P, ctypes.POINTER(ServerStats)]
+        L.rmq_server_fail_next_batches.argtypes = [_P, ctypes.c_uint32]
+        L.rmq_serve_serial_loop.argtypes = [_P, _U64, _P, _U64, _P, _P, _P, ctypes.POINTER(ctypes.c_double)]
         L.rmq_server_destroy.argtypes = [_P]
         L.rmq_server_destroy.restype = None
         _server_bound = True
@@ -675,6 +697,14 @@ class Server:
             raise RMQError(st, "rmq_server_replay")
         return lat, float(wall.value)
 
+    def fail_next_batches(self, count: int) -> None:
+        """Host-side fault injection: the next `count` batches fail as if
+        their upload had returned a CUDA error (their requests get
+        RMQ_ERR_CUDA)."""
+        st = _bind_server().rmq_server_fail_next_batches(self._h, int(count))
+        if st != RMQ_OK:
+            raise RMQError(st, "rmq_server_fail_next_batches")
+
     def stats(self) -> dict:
         s = ServerStats()
         st = _bind_server().rmq_server_get_stats(self._h, ctypes.byref(s))
@@ -699,3 +729,22 @@ class Server:
 
     def __exit__(self, *exc):
         self.close()
+
+
+def serve_serial_loop(handles, events: np.ndarray, lr: np.ndarray, out_idx: np.ndarray,
+                      out_min: np.ndarray | None = None) -> float:
+    """The server's comparator: the events' query requests one after another
+    through rmq_query_idx_host on prebuilt handles (one Hierarchy per array
+    id); returns the loop's wall time in seconds."""
+    assert events.dtype == TRACE_DTYPE
+    arr = (_P * len(handles))(*[h.handle for h in handles])
+    wall = ctypes.c_double()
+    st = _bind_server().rmq_serve_serial_loop(arr, len(handles), events.ctypes.data, events.size,
+                                              lr.ctypes.data if hasattr(lr, "ctypes") else int(lr.data_ptr()),
+                                              out_idx.ctypes.data if hasattr(out_idx, "ctypes") else int(out_idx.data_ptr()),
+                                              (out_min.ctypes.data if hasattr(out_min, "ctypes") else int(out_min.data_ptr()))
+                                              if out_min is not None else None,
+                                              ctypes.byref(wall))
+    if st != RMQ_OK:
+        raise RMQError(st, "rmq_serve_serial_loop")
+    return float(wall.value)

@@ -162,8 +162,14 @@ const char* rmq_strerror(int status);
  * the library holds until the process exits; then the queries are answered,
  * both on `stream`.  Limit: n <= 2^22 (4,194,304 entries); a larger n, or a t
  * whose levels do not fit, returns RMQ_ERR_UNSUPPORTED before any device
- * work.  The first call on each device looks up the array's device address
- * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * work.  The first call on each device (each device context: after a
+ * cudaDeviceReset the next call counts as a first call again) looks up the
+ * array's device address (cudaGetSymbolAddress).  CUDA loads device code
+ * lazily by default, so that first call is also what places the array and
+ * the kernels of this entry point on the device and may need device memory
+ * for them: make it before reserving the whole device for a pool, and
+ * before any stream capture (a call with q = 0 places the array and the
+ * build kernel; one with q > 0 also the query kernel).
  * All calls on a device share the array, which keeps the last call's
  * contents (each call rewrites every entry it reads, so nothing needs
  * clearing): calls whose device work overlaps, on different streams or from
@@ -179,6 +185,17 @@ int rmq_query_idx_static(const float* d_values, uint64_t n, uint64_t scan_thresh
  * skipped, not made), then the count is cleared.  The regular library
  * returns RMQ_ERR_UNSUPPORTED. */
 int rmq_debug_bounds_violations(uint64_t* count);
+
+/* Measurement aid, no counterpart in the reference: the rate at which this
+ * GPU's SMs read L2-resident 32-byte sectors with the query kernels' load
+ * form, the bound of the coarse levels' reads.  Reads d_buf[0 .. bytes)
+ * (bytes / 32 a power of two, at least 1024; the buffer should fit in L2 and
+ * hold values >= -1) once to bring it into L2, then `passes` more times,
+ * in address order (random = 0) or at hashed sector positions (random = 1),
+ * on `stream`; *ms_out = device time of those passes (CUDA events).  Blocks
+ * until done. */
+int rmq_measure_l2_read(const float* d_buf, uint64_t bytes, uint32_t passes, int32_t random,
+                        rmq_stream_t stream, float* ms_out);
 
 /* Level layout only (host computation, no device work): the reference's rule
  * (src/xxx.h:225-243) generalised to rf = 2^rf_log.  Returns RMQ_ERR_ARG when

@@ -64,6 +64,15 @@ int rmq_batch_query(rmq_batch* b, rmq_stream_t stream);
  * rmq_batch_set_queries / rmq_batch_autotune, replayed afterwards). */
 int rmq_batch_run(rmq_batch* b, rmq_stream_t stream);
 
+/* The comparator of the batched form: the same work as a per-array loop of
+ * the plain single-array kernels, the way a caller without this header would
+ * run it with buffers allocated up front.  For each array in turn, the
+ * single-array build (the kernels of rmq_build) into the batch's own level
+ * buffers, then the single-array query kernel of rmq_query_idx over its
+ * queries; all on `stream`, nothing synchronised between arrays.  Results
+ * are identical to rmq_batch_run's. */
+int rmq_batch_run_per_array(rmq_batch* b, rmq_stream_t stream);
+
 /* Autotuner: times the query kernel on the registered queries for each
  * candidate scan threshold t in {16, 32, 64, 256, 1024} and CTA size in
  * {64, 128, 256, 512} threads, keeps the fastest and rebuilds with it.

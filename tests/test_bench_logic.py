@@ -134,3 +134,35 @@ def test_reference_arm_line_on_cpu():
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
     assert line["config"]["workload"].startswith("plain single array")
+
+
+def test_reference_arm_maps_no_product_library():
+    """The reference arm gets its inputs from the oracle's own generators:
+    no library of the product package is mapped into its process."""
+    import subprocess
+    import sys
+    from pathlib import Path
+    root = Path(__file__).resolve().parents[1]
+    code = ("import sys; sys.path.insert(0, %r); import bench; "
+            "bench.main(['--impl', 'reference', '--steps', '1', '--warmup', '3', '--n', '4096', '--q', '512', "
+            "'--lr', '-7', '--ref-step-queries', '128']); "
+            "maps = open('/proc/self/maps').read(); "
+            "print('PRODUCT-MAPPED' if 'gpu-rmq_gb300' in maps else 'NO-PRODUCT-LIBRARY')" % str(root))
+    out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=300, cwd=root)
+    assert out.returncode == 0, out.stderr[-2000:]
+    assert out.stdout.strip().splitlines()[-1] == "NO-PRODUCT-LIBRARY"
+
+
+def test_sub_record_selection():
+    assert bench.selected_sub_records("none") == []
+    assert bench.selected_sub_records("all") == bench.SUB_RECORDS
+    assert bench.selected_sub_records("c1_n2e20,served_c5") == ["c1_n2e20", "served_c5"]
+    with pytest.raises(SystemExit):
+        bench.selected_sub_records("c9")
+
+
+def test_cpu_list_and_numa_maps_parsing():
+    assert bench._cpulist("0-3,8,10-11") == {0, 1, 2, 3, 8, 10, 11}
+    a = np.ones(1 << 20, dtype=np.float32)  # a mapping of its own
+    nodes = bench.buffer_nodes(a.ctypes.data)
+    assert isinstance(nodes, dict)

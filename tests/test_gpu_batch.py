@@ -182,3 +182,28 @@ def test_tuning_cache_and_set_tuning(cuda, tmp_path):
         b.run()
         torch.cuda.synchronize()
         _check(out_min, out_idx, emin, eidx, "set_tuning(32, 512)")
+
+
+def test_per_array_loop_matches_batched(cuda):
+    """rmq_batch_run_per_array (the per-array loop of the plain build and
+    query kernels over the batch's buffers) gives the batched results, which
+    are the oracle's."""
+    import torch
+    rng = np.random.default_rng(9)
+    sizes = [1, 8, 9, 8193, 100_003] + [int(x) for x in np.exp(rng.uniform(np.log(1 << 10), np.log(1 << 19), 30))]
+    dv, dq, offs, arrays, qs, qo = _make_batch(cuda, sizes, 9)
+    emin, eidx = _expected(arrays, qs, qo)
+    q = qs.shape[0]
+    out_min = torch.empty(q, dtype=torch.float32, device=cuda)
+    out_idx = torch.empty(q, dtype=torch.int32, device=cuda)
+    with R.Batch(dv, offs, sizes, t=32) as b:
+        b.set_queries(dq, qo, out_idx, out_min)
+        for rep in range(2):
+            out_min.fill_(-1)
+            out_idx.fill_(-1)
+            b.run_per_array()
+            torch.cuda.synchronize()
+            _check(out_min, out_idx, emin, eidx, f"per-array loop {rep}")
+        b.run()
+        torch.cuda.synchronize()
+        _check(out_min, out_idx, emin, eidx, "graph after the loop")

@@ -113,3 +113,45 @@ def test_invalid_query_and_replay(cuda):
         lat, wall = srv.replay(ev, lr, out_i, out_m)
         assert lat[1] == -1 and (lat[[0, 2, 3]] > 0).all() and wall > 0
         assert np.array_equal(out_i[:2000], oracle.rmq_argmin(a, lr[:2000]))
+
+
+def test_serial_loop_comparator_matches_oracle(cuda):
+    """rmq_serve_serial_loop (the server's per-request comparator) answers
+    every query request of a trace exactly, from page-locked and from
+    ordinary host buffers."""
+    import torch
+    rng = np.random.default_rng(12)
+    sizes = [5000, 1 << 16, 70_001]
+    arrays = [rng.random(n).astype(np.float32) for n in sizes]
+    hs = [R.Hierarchy(torch.from_numpy(a).to(cuda), variant="vl", t=64) for a in arrays]
+    ev = np.zeros(12, dtype=R.TRACE_DTYPE)
+    parts, off = [], 0
+    for i in range(ev.size):
+        if i == 5:
+            ev["kind"][i] = 1  # a registration: skipped by the loop
+            continue
+        aid = int(rng.integers(0, len(sizes)))
+        qs = _queries(rng, sizes[aid], int(rng.integers(1, 3000)))
+        ev["array_id"][i], ev["q_offset"][i], ev["q"][i] = aid, off, qs.shape[0]
+        parts.append(qs)
+        off += qs.shape[0]
+    lr = np.ascontiguousarray(np.concatenate(parts))
+    for pinned in (True, False):
+        if pinned:
+            h_lr = torch.from_numpy(lr.view(np.int32).reshape(-1)).pin_memory()
+            oi = torch.zeros(off, dtype=torch.int32).pin_memory()
+            om = torch.zeros(off, dtype=torch.float32).pin_memory()
+        else:
+            h_lr, oi, om = lr, np.zeros(off, np.uint32), np.zeros(off, np.float32)
+        wall = R.serve_serial_loop(hs, ev, h_lr, oi, om)
+        assert wall > 0
+        gi = oi.numpy().view(np.uint32) if pinned else oi
+        gm = om.numpy() if pinned else om
+        for i in range(ev.size):
+            if ev["kind"][i] != 0:
+                continue
+            o, q, aid = int(ev["q_offset"][i]), int(ev["q"][i]), int(ev["array_id"][i])
+            assert np.array_equal(gi[o:o + q], oracle.rmq_argmin(arrays[aid], lr[o:o + q]))
+            assert gm[o:o + q].tobytes() == oracle.rmq_min(arrays[aid], lr[o:o + q]).tobytes()
+    for h in hs:
+        h.close()
