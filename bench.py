@@ -1014,6 +1014,8 @@ def batched_record(args, ws, rank, dev) -> dict:
         "arrays": A, "total_values": total, "total_queries": Q, "seed": args.seed,
         "l2": "inputs larger than L2 (no flush)", "data": "synthetic (device counter-based generators)",
         "autotuned": {"scan_threshold": int(tuned.scan_threshold), "query_block": int(tuned.query_block),
+                      "class_threshold": [int(x) for x in tuned.class_threshold],
+                      "class_upper_entries": ["2^14", "2^18", "any"],
                       "query_ms": float(tuned.query_ms)},
         "build_ms": build_ms, "query_ms": query_ms,
         "loop_plain_kernels": {"value": loop_value, "ms_per_step": loop_ms, "steps": loop_steps,
@@ -1102,16 +1104,32 @@ def served_record(args, ws, rank, dev) -> dict:
     import rmq_gb300 as R
     from oracle import oracle
 
+    phase = {}
+    tp = time.perf_counter()
+
+    def mark(name):
+        nonlocal tp
+        now = time.perf_counter()
+        phase[name] = round(now - tp, 3)
+        tp = now
+
     rng = np.random.default_rng(args.seed + rank)
     sizes = [int(np.exp(rng.uniform(np.log(2.0 ** 16), np.log(2.0 ** 26)))) for _ in range(256)]
     seed_of = lambda a: args.seed * 1000003 + a  # noqa: E731  (the trace uses the same rule)
-    ev, lr, n_of = serve_trace(rng, sizes, args.serve_seconds, 20000.0, 0.05, args.seed)
+    ev, lr_pageable, n_of = serve_trace(rng, sizes, args.serve_seconds, 20000.0, 0.05, args.seed)
     req = ev["kind"] == 0
     Q = int(ev["q"][req].sum())
-    # Result buffers written once up front: the replay then measures the
-    # server, not the first-touch page faults of fresh host memory.
-    out_i = np.ones(Q, dtype=np.uint32)
-    out_m = np.ones(Q, dtype=np.float32)
+    mark("trace")
+    # The request buffers are page-locked (the server then reads the queries
+    # and writes the results in place), and written once up front: the replay
+    # measures the server, not first-touch page faults of fresh host memory.
+    lr_t = torch.from_numpy(lr_pageable.view(np.int32).reshape(-1)).pin_memory()
+    lr = lr_t.numpy().view(np.uint32).reshape(-1, 2)
+    out_i_t = torch.ones(Q, dtype=torch.int32).pin_memory()
+    out_m_t = torch.ones(Q, dtype=torch.float32).pin_memory()
+    out_i = out_i_t.numpy().view(np.uint32)
+    out_m = out_m_t.numpy()
+    mark("pin_buffers")
 
     # Warm-up on a throwaway server (a 0.2 s trace over 32 small arrays): the
     # first serving run of a process otherwise carries a cold tail (first
@@ -1125,6 +1143,7 @@ def served_record(args, ws, rank, dev) -> dict:
             wsrv.register_generated(n, args.seed + 7919 + a)
         wq = int(wev["q"][wev["kind"] == 0].sum())
         wsrv.replay(wev, wlr, np.empty(wq, np.uint32), np.empty(wq, np.float32))
+    mark("warmup_server")
 
     srv = R.Server(hbm_budget_bytes=64 << 30, slots=args.serve_slots, t=64, query_threads=args.serve_threads)
     for a, n in enumerate(sizes):
@@ -1133,10 +1152,12 @@ def served_record(args, ws, rank, dev) -> dict:
     wi, wm = np.empty(1, np.uint32), np.empty(1, np.float32)
     for a in range(len(sizes)):
         srv.wait(srv.submit(a, warm, wi, wm))  # every initial array built
+    mark("register")
     with ClockSampler(dev.index) as clocks:
         lat, wall = srv.replay(ev, lr, out_i, out_m)
     st = srv.stats()
     lat_req = lat[req & (lat >= 0)]
+    mark("replay")
 
     # parity: a sample of requests on the smaller arrays against the CPU oracle
     parity = True
@@ -1149,12 +1170,15 @@ def served_record(args, ws, rank, dev) -> dict:
         parity &= np.array_equal(out_i[o:o + q], oracle.rmq_argmin(x, lr[o:o + q]))
         parity &= out_m[o:o + q].tobytes() == oracle.rmq_min(x, lr[o:o + q]).tobytes()
 
+    mark("parity")
     # capacity: requests on the initial arrays, all issued at once
     cap_ev = ev[req & (ev["array_id"] < len(sizes))].copy()
     cap_ev["t_arrival_s"] = 0.0
     cap_q = int(cap_ev["q"].sum())
     _, cap_wall = srv.replay(cap_ev, lr, out_i, out_m)
+    cap_stats = srv.stats()
     srv.close()
+    mark("capacity")
 
     # the comparator: a C-side per-request loop of the plain kernel on
     # prebuilt handles, with page-locked host buffers (rmq_query_idx_host's
@@ -1167,21 +1191,20 @@ def served_record(args, ws, rank, dev) -> dict:
         R.gen_values_device(v, seed_of(a))
         vals.append(v)
         hs.append(R.Hierarchy(v, variant="vl", t=64, stream=stream))
-    h_lr = torch.from_numpy(lr.view(np.int32).reshape(-1)).pin_memory()
-    h_i = torch.empty(Q, dtype=torch.int32).pin_memory()
-    h_m = torch.empty(Q, dtype=torch.float32).pin_memory()
-    h_i.fill_(1)
-    h_m.fill_(1.0)
+    h_i = torch.ones(Q, dtype=torch.int32).pin_memory()
+    h_m = torch.ones(Q, dtype=torch.float32).pin_memory()
     torch.cuda.synchronize()
-    R.serve_serial_loop(hs, cap_ev[:64], h_lr, h_i, h_m)  # warm-up
-    loop_s = R.serve_serial_loop(hs, cap_ev, h_lr, h_i, h_m)
+    mark("loop_setup")
+    R.serve_serial_loop(hs, cap_ev[:64], lr_t, h_i, h_m)  # warm-up
+    loop_s = R.serve_serial_loop(hs, cap_ev, lr_t, h_i, h_m)
     loop_same = True
     for e in cap_ev[:: max(1, cap_ev.size // 64)]:
         o, q = int(e["q_offset"]), int(e["q"])
         loop_same &= bool(np.array_equal(h_i[o:o + q].numpy().view(np.uint32), out_i[o:o + q]))
     for h in hs:
         h.close()
-    del vals, h_lr, h_i, h_m
+    del vals, h_i, h_m
+    mark("loop")
 
     return {
         "metric": "RMQ queries/s (served: continuous batching)", "value": Q / wall, "unit": UNIT,
@@ -1198,7 +1221,11 @@ def served_record(args, ws, rank, dev) -> dict:
         "offered_queries_per_s": Q / float(ev["t_arrival_s"][-1]),
         "server_stats": st,
         "capacity": {"value": cap_q / cap_wall, "requests": int(cap_ev.size), "queries": cap_q,
-                     "what": "same requests on the initial arrays, all arriving at once"},
+                     "what": "same requests on the initial arrays, all arriving at once",
+                     "batches": int(cap_stats["batches"] - st["batches"]),
+                     "requests_answered_in_place": int(cap_stats["direct_requests"] - st["direct_requests"])},
+        "request_buffers": "page-locked (queries read and results written in place by the batch kernel)",
+        "phase_s": phase,
         "loop_plain_kernel": {"value": cap_q / loop_s, "seconds": loop_s, "results_equal_served": loop_same,
                               "what": "rmq_serve_serial_loop (C side): per request rmq_query_idx_host on a "
                                       "prebuilt handle, page-locked buffers, waited for before the next"},

@@ -140,6 +140,67 @@ batch_query_kernel(const float* __restrict__ values, const ArrayDesc* __restrict
                      ARGMIN ? out_idx + at : nullptr, nullptr);
 }
 
+// The served batch's kernel: as batch_query_kernel, but every entry (a
+// request) reads its queries and writes its results through its own ServeIO
+// (staging buffers or the request's page-locked host buffers), and counts
+// its invalid queries so the host needs no pass over the results.
+template <int R>
+__global__ void __launch_bounds__(kMaxQueryThreads)
+serve_query_kernel(const float* __restrict__ values, const ArrayDesc* __restrict__ descs,
+                   const uint32_t* __restrict__ unit_owner, const uint64_t* __restrict__ unit_off,
+                   const uint64_t* __restrict__ q_off, uint64_t total_units,
+                   const float* __restrict__ lvl_val, const uint32_t* __restrict__ lvl_idx,
+                   const ServeIO* __restrict__ io, uint32_t* __restrict__ bad) {
+    __shared__ Levels wlv[kMaxQueryThreads / 32];
+    __shared__ uint64_t wq[kMaxQueryThreads / 32][2];
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const uint64_t unit = uint64_t(blockIdx.x) * (blockDim.x >> 5) + warp;
+    if (unit >= total_units) return;  // the whole warp leaves
+    const uint32_t a = __ldg(unit_owner + unit);
+    const ArrayDesc& d = descs[a];
+    Levels& lv = wlv[warp];
+    const uint32_t nl = d.num_levels;
+    if (lane < uint32_t(kMaxLevels)) {
+        const uint32_t k = lane;
+        const bool has = k > 0 && k < nl;
+        lv.val[k] = k == 0 ? values + d.val_off : (has ? lvl_val + d.lvl_base + d.off[k] : nullptr);
+        lv.idx[k] = (has && lvl_idx != nullptr) ? lvl_idx + d.idx_base + d.off[k] : nullptr;
+        lv.size[k] = k < nl ? d.size[k] : 0u;
+    } else if (lane == 31) {
+        lv.num_levels = nl;
+        const uint64_t q0 = (unit - unit_off[a]) * kUnitQueries;  // local to the request
+        const uint64_t qe = q0 + kUnitQueries;
+        const uint64_t q1 = q_off[a + 1] - q_off[a];
+        wq[warp][0] = q0;
+        wq[warp][1] = qe < q1 ? qe : q1;
+    }
+    __syncwarp();
+    const ServeIO r = io[a];
+    const uint64_t q0 = wq[warp][0];
+    const uint32_t cnt = uint32_t(wq[warp][1] - q0);
+    const bool in_range = lane < cnt;
+    uint2 Q = make_uint2(1u, 0u);
+    if (in_range) Q = ld_query(r.qs + q0 + lane);
+    float v;
+    uint32_t idx;
+    const bool valid = vl_compute<R, true>(lv, Q, in_range, v, idx);
+    if (in_range) {
+        if (r.out_min != nullptr) st_stream(r.out_min + q0 + lane, v);
+        if (r.out_idx != nullptr) st_stream(r.out_idx + q0 + lane, idx);
+    }
+    const uint32_t nbad = __popc(__ballot_sync(0xffffffffu, in_range && !valid));
+    if (lane == 0 && nbad != 0) atomicAdd(bad + a, nbad);
+}
+
+cudaError_t launch_serve_query(const ServeQueryArgs& a, cudaStream_t s) {
+    if (a.total_units == 0) return cudaSuccess;
+    const uint32_t warps = a.threads / 32u;
+    const uint32_t grid = uint32_t((a.total_units + warps - 1) / warps);
+    serve_query_kernel<3><<<grid, a.threads, 0, s>>>(a.values, a.descs, a.owner, a.unit_off, a.q_off,
+                                                     a.total_units, a.lvl_val, a.lvl_idx, a.io, a.bad);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_fill_owner(const uint64_t* unit_off, uint32_t num, uint32_t* owner, cudaStream_t s) {
     if (num == 0) return cudaSuccess;
     fill_owner_kernel<<<num, 256, 0, s>>>(unit_off, owner);
@@ -174,7 +235,8 @@ struct rmq_batch {
     const float* d_values = nullptr;
     uint32_t num_arrays = 0;
     std::vector<uint64_t> val_off, sizes;
-    uint64_t t = 64;
+    uint64_t t = 64;        // scan threshold of the largest size class (the batch-wide t when uniform)
+    uint64_t tc[3] = {64, 64, 64};  // scan threshold per size class (rmq_batch_info.class_upper)
     uint32_t qblock = 128;  // threads per CTA of the query kernel (untuned default)
     int with_index = 1;
     int device = 0;
@@ -211,6 +273,16 @@ namespace {
 
 constexpr uint64_t kBatchDefaultT = 64;
 constexpr uint64_t kTuneT[] = {16, 32, 64, 256, 1024};
+// Size classes of the per-class thresholds: arrays below 2^14 entries, below
+// 2^18, and the rest.
+constexpr int kClasses = 3;
+constexpr uint64_t kClassUpper[kClasses] = {uint64_t(1) << 14, uint64_t(1) << 18, ~uint64_t(0)};
+
+int size_class(uint64_t n) {
+    int c = 0;
+    while (c + 1 < kClasses && n >= kClassUpper[c]) ++c;
+    return c;
+}
 constexpr uint32_t kTuneBlock[] = {64, 128, 256, 512};  // threads per CTA of the query kernel
 
 int status_of(cudaError_t e) {
@@ -231,14 +303,15 @@ void drop_graph(rmq_batch* b) {
     }
 }
 
-// Lays out every array with threshold t, uploads descriptors and tile offsets.
-int plan(rmq_batch* b, uint64_t t, cudaStream_t s) {
+// Lays out every array with its size class's threshold tc[class], uploads
+// descriptors and tile offsets.
+int plan(rmq_batch* b, const uint64_t (&tc)[kClasses], cudaStream_t s) {
     std::vector<ArrayDesc> descs(b->num_arrays);
     std::vector<uint64_t> tile_off(b->num_arrays + 1, 0);
     uint64_t base = 0;
     uint32_t max_levels = 1;
     for (uint32_t a = 0; a < b->num_arrays; ++a) {
-        const rmq::Layout lay = rmq::plan_layout(b->sizes[a], t, 3);
+        const rmq::Layout lay = rmq::plan_layout(b->sizes[a], tc[size_class(b->sizes[a])], 3);
         ArrayDesc& d = descs[a];
         std::memset(&d, 0, sizeof(d));
         d.val_off = b->val_off[a];
@@ -263,12 +336,18 @@ int plan(rmq_batch* b, uint64_t t, cudaStream_t s) {
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);  // tile_off dies here; descs are kept
     if (e != cudaSuccess) return status_of(e);
     b->h_descs.swap(descs);
-    b->t = t;
+    for (int c = 0; c < kClasses; ++c) b->tc[c] = tc[c];
+    b->t = tc[kClasses - 1];
     b->lvl_used = base;
     b->max_levels = max_levels;
     b->total_tiles = tile_off[b->num_arrays];
     drop_graph(b);
     return RMQ_OK;
+}
+
+int plan(rmq_batch* b, uint64_t t, cudaStream_t s) {
+    const uint64_t tc[kClasses] = {t, t, t};
+    return plan(b, tc, s);
 }
 
 int upload_blocks(rmq_batch* b, cudaStream_t s) {
@@ -474,7 +553,7 @@ int rmq_batch_run_per_array(rmq_batch* b, rmq_stream_t stream) {
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     for (uint32_t a = 0; a < b->num_arrays; ++a) {
         const ArrayDesc& d = b->h_descs[a];
-        const rmq::Layout lay = rmq::plan_layout(b->sizes[a], b->t, 3);
+        const rmq::Layout lay = rmq::plan_layout(b->sizes[a], b->tc[size_class(b->sizes[a])], 3);
         const float* vals = b->d_values + d.val_off;
         float* lvl = b->lvl_val + d.lvl_base;
         uint32_t* idx = b->lvl_idx != nullptr ? b->lvl_idx + d.idx_base : nullptr;
@@ -503,11 +582,27 @@ int rmq_batch_run_per_array(rmq_batch* b, rmq_stream_t stream) {
     return RMQ_OK;
 }
 
+// Device time of one query pass with the current plan and CTA size (one
+// warm-up launch, then the mean of `reps` timed launches).
+int time_query(rmq_batch* b, cudaStream_t s, int reps, float* ms_out) {
+    cudaError_t e = enqueue_query(b, s);  // warm-up
+    if (e == cudaSuccess) e = cudaEventRecord(b->ev0, s);
+    for (int rep = 0; rep < reps && e == cudaSuccess; ++rep) e = enqueue_query(b, s);
+    if (e == cudaSuccess) e = cudaEventRecord(b->ev1, s);
+    if (e == cudaSuccess) e = cudaEventSynchronize(b->ev1);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, b->ev0, b->ev1);
+    if (e != cudaSuccess) return status_of(e);
+    *ms_out = ms / float(reps);
+    return RMQ_OK;
+}
+
 int rmq_batch_autotune(rmq_batch* b, rmq_stream_t stream, rmq_batch_info* info) {
     rmq::NvtxRange nvtx_range("rmq_batch_autotune");
     if (b == nullptr || !b->queries_set) return RMQ_ERR_ARG;
     DeviceGuard guard(b->device);
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    // 1. one threshold for every array x CTA size
     float best = -1.f;
     uint64_t best_t = b->t;
     uint32_t best_block = b->qblock;
@@ -520,17 +615,9 @@ int rmq_batch_autotune(rmq_batch* b, rmq_stream_t stream, rmq_batch_info* info) 
             b->qblock = qb;
             st = upload_blocks(b, s);
             if (st != RMQ_OK) return st;
-            e = enqueue_query(b, s);  // warm-up
-            for (int rep = 0; rep < 3 && e == cudaSuccess; ++rep) {
-                if (rep == 1) e = cudaEventRecord(b->ev0, s);
-                if (e == cudaSuccess) e = enqueue_query(b, s);
-            }
-            if (e == cudaSuccess) e = cudaEventRecord(b->ev1, s);
-            if (e == cudaSuccess) e = cudaEventSynchronize(b->ev1);
             float ms = 0.f;
-            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, b->ev0, b->ev1);
-            if (e != cudaSuccess) return status_of(e);
-            ms *= 0.5f;  // two timed launches
+            st = time_query(b, s, 2, &ms);
+            if (st != RMQ_OK) return st;
             if (best < 0.f || ms < best) {
                 best = ms;
                 best_t = t;
@@ -538,10 +625,32 @@ int rmq_batch_autotune(rmq_batch* b, rmq_stream_t stream, rmq_batch_info* info) 
             }
         }
     }
-    int st = plan(b, best_t, s);
-    if (st != RMQ_OK) return st;
+    // 2. each size class's threshold in turn (largest arrays first, they
+    // carry most of the queries), the others held; a change is kept only
+    // when it is faster by more than 0.5 %, above the timing noise.
     b->qblock = best_block;
-    st = upload_blocks(b, s);
+    int st = upload_blocks(b, s);
+    if (st != RMQ_OK) return st;
+    uint64_t best_tc[kClasses] = {best_t, best_t, best_t};
+    for (int c = kClasses - 1; c >= 0; --c) {
+        for (uint64_t t : kTuneT) {
+            if (t == best_tc[c]) continue;
+            uint64_t tc[kClasses] = {best_tc[0], best_tc[1], best_tc[2]};
+            tc[c] = t;
+            st = plan(b, tc, s);
+            if (st != RMQ_OK) return st;
+            cudaError_t e = enqueue_build(b, s);
+            if (e != cudaSuccess) return status_of(e);
+            float ms = 0.f;
+            st = time_query(b, s, 2, &ms);
+            if (st != RMQ_OK) return st;
+            if (ms < best * 0.995f) {
+                best = ms;
+                best_tc[c] = t;
+            }
+        }
+    }
+    st = plan(b, best_tc, s);
     if (st != RMQ_OK) return st;
     cudaError_t e = enqueue_build(b, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
@@ -558,6 +667,30 @@ int rmq_batch_set_tuning(rmq_batch* b, uint64_t scan_threshold, uint32_t query_b
     DeviceGuard guard(b->device);
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     int st = plan(b, scan_threshold, s);  // RMQ_ERR_UNSUPPORTED when the levels would not fit
+    if (st != RMQ_OK) return st;
+    b->qblock = query_block;
+    if (b->queries_set) {
+        st = upload_blocks(b, s);
+        if (st != RMQ_OK) return st;
+    }
+    drop_graph(b);
+    b->build_timed = false;
+    return RMQ_OK;
+}
+
+int rmq_batch_set_class_tuning(rmq_batch* b, const uint64_t* class_thresholds, uint32_t query_block,
+                               rmq_stream_t stream) {
+    if (b == nullptr || class_thresholds == nullptr || query_block < 32 || query_block > rmq::kMaxQueryThreads ||
+        query_block % 32 != 0)
+        return RMQ_ERR_ARG;
+    uint64_t tc[kClasses];
+    for (int c = 0; c < kClasses; ++c) {
+        if (class_thresholds[c] < 8) return RMQ_ERR_ARG;
+        tc[c] = class_thresholds[c];
+    }
+    DeviceGuard guard(b->device);
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    int st = plan(b, tc, s);  // RMQ_ERR_UNSUPPORTED when the levels would not fit
     if (st != RMQ_OK) return st;
     b->qblock = query_block;
     if (b->queries_set) {
@@ -587,6 +720,10 @@ int rmq_batch_get_info(const rmq_batch* bc, rmq_batch_info* info) {
     }
     info->build_ms = b->build_ms;
     info->query_ms = b->query_ms;
+    for (int c = 0; c < kClasses; ++c) {
+        info->class_threshold[c] = b->tc[c];
+        info->class_upper[c] = kClassUpper[c];
+    }
     return RMQ_OK;
 }
 

@@ -79,6 +79,35 @@ struct BatchQueryArgs {
 };
 
 cudaError_t launch_batch_query(const BatchQueryArgs& a, cudaStream_t s);
+
+// Where one served request's queries come from and its results go: device
+// staging buffers, or the request's own page-locked host buffers, which the
+// kernel reads and writes directly over the CPU-GPU link.  Either result
+// pointer may be null.
+struct ServeIO {
+    const uint2* qs;
+    uint32_t* out_idx;
+    float* out_min;
+};
+
+// The served batch: entry e (a request) answers its q_off[e+1] - q_off[e]
+// queries through io[e] and counts its invalid queries in bad[e] (zeroed by
+// the caller); units of 32 queries as for launch_batch_query.
+struct ServeQueryArgs {
+    const float* values;
+    const ArrayDesc* descs;
+    const uint32_t* owner;
+    const uint64_t* unit_off;
+    const uint64_t* q_off;
+    uint64_t total_units;
+    const float* lvl_val;
+    const uint32_t* lvl_idx;
+    const ServeIO* io;
+    uint32_t* bad;
+    uint32_t threads;  // CTA size, multiple of 32, <= 512
+};
+
+cudaError_t launch_serve_query(const ServeQueryArgs& a, cudaStream_t s);
 cudaError_t launch_fill_owner(const uint64_t* unit_off, uint32_t num, uint32_t* owner, cudaStream_t s);
 
 #if RMQ_DEBUG_BOUNDS

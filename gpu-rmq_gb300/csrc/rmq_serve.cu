@@ -65,6 +65,12 @@ struct Request {
     uint64_t q = 0;
     uint32_t* h_idx = nullptr;
     float* h_min = nullptr;
+    // Page-locked request buffers: their device-side addresses, through which
+    // the kernel reads the queries and writes the results in place.
+    bool direct = false;
+    const uint32_t* d_lr = nullptr;
+    uint32_t* d_idx = nullptr;
+    float* d_min = nullptr;
     Clock::time_point t_submit, t_done;
     int status = RMQ_OK;
     bool done = false;
@@ -74,26 +80,48 @@ struct Slot {
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
     // One upload and one download per batch: in = descs | q_off | unit_off |
-    // owner of each 32-query unit | queries (sized by the batch);
-    // out = argmin[nq] | min[nq].
+    // io | owner of each 32-query unit | the staged requests' queries (sized
+    // by the batch); out = invalid-query count per request | the staged
+    // requests' argmin | their minima.  Requests with page-locked buffers
+    // are read and written in place and take no staging.
     uint8_t* h_in = nullptr;   // pinned
     uint8_t* h_out = nullptr;  // pinned
     uint8_t* d_in = nullptr;
     uint8_t* d_out = nullptr;
-    uint64_t nq = 0;           // queries of the batch in flight
+    uint64_t snq = 0;          // staged queries of the batch in flight
+    uint32_t nr = 0;
     std::vector<uint64_t> reqs;
     std::vector<Request*> rptr;     // stable element pointers (taken under the lock)
-    std::vector<uint64_t> req_off;  // query offset of each request in the batch
+    std::vector<uint64_t> req_off;  // staged query offset of each staged request
     bool busy = false;
 };
 
 // Bytes of a batch's header for nr requests, rounded to 16 (the owner table
-// follows), and of its owner table for `units` work units (the queries follow).
+// follows), of its owner table for `units` work units (the staged queries
+// follow), and of the invalid-query counts at the head of the download.
 size_t header_bytes(uint32_t nr) {
-    const size_t b = size_t(nr) * sizeof(rmq::ArrayDesc) + 2 * size_t(nr + 1) * sizeof(uint64_t);
+    const size_t b = size_t(nr) * sizeof(rmq::ArrayDesc) + 2 * size_t(nr + 1) * sizeof(uint64_t) +
+                     size_t(nr) * sizeof(rmq::ServeIO);
     return (b + 15) & ~size_t(15);
 }
 size_t owner_bytes(uint64_t units) { return (units * sizeof(uint32_t) + 15) & ~size_t(15); }
+size_t bad_bytes(uint32_t nr) { return (size_t(nr) * sizeof(uint32_t) + 15) & ~size_t(15); }
+
+// The device-side address of page-locked host memory [p, p + bytes), or null
+// when that range is not wholly page-locked and mapped (or p is null).
+void* mapped_range(const void* p, size_t bytes, size_t align) {
+    if (p == nullptr || bytes == 0 || (reinterpret_cast<uintptr_t>(p) & (align - 1)) != 0) return nullptr;
+    cudaPointerAttributes a0, a1;
+    const char* last = static_cast<const char*>(p) + bytes - 1;
+    if (cudaPointerGetAttributes(&a0, p) != cudaSuccess || cudaPointerGetAttributes(&a1, last) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a0.type != cudaMemoryTypeHost || a1.type != cudaMemoryTypeHost || a0.devicePointer == nullptr ||
+        a1.devicePointer != static_cast<char*>(a0.devicePointer) + (bytes - 1))
+        return nullptr;
+    return a0.devicePointer;
+}
 
 }  // namespace
 
@@ -195,8 +223,9 @@ bool admit(rmq_server* s, uint64_t id) {
 // the other.
 void finish_slot(rmq_server* s, Slot& sl, int failed = RMQ_OK) {
     std::vector<int> status(sl.reqs.size(), failed);
-    const uint32_t* h_idx = reinterpret_cast<const uint32_t*>(sl.h_out);
-    const float* h_min = reinterpret_cast<const float*>(sl.h_out + sl.nq * sizeof(uint32_t));
+    const uint32_t* bad = reinterpret_cast<const uint32_t*>(sl.h_out);
+    const uint32_t* h_idx = reinterpret_cast<const uint32_t*>(sl.h_out + bad_bytes(sl.nr));
+    const float* h_min = reinterpret_cast<const float*>(sl.h_out + bad_bytes(sl.nr) + sl.snq * sizeof(uint32_t));
     for (size_t i = 0; i < sl.reqs.size(); ++i) {
         Request& r = *sl.rptr[i];
         if (failed != RMQ_OK) {
@@ -206,15 +235,11 @@ void finish_slot(rmq_server* s, Slot& sl, int failed = RMQ_OK) {
             }
             continue;
         }
+        if (bad[i] != 0) status[i] = RMQ_ERR_QUERY_RANGE;
+        if (r.direct) continue;  // results already in place
         const uint64_t o = sl.req_off[i];
         if (r.h_idx != nullptr) std::memcpy(r.h_idx, h_idx + o, r.q * sizeof(uint32_t));
         if (r.h_min != nullptr) std::memcpy(r.h_min, h_min + o, r.q * sizeof(float));
-        for (uint64_t j = 0; j < r.q; ++j) {
-            if (h_idx[o + j] == rmq::kNoPos) {
-                status[i] = RMQ_ERR_QUERY_RANGE;
-                break;
-            }
-        }
     }
     const Clock::time_point now = Clock::now();
     std::lock_guard<std::mutex> lock(s->mu);
@@ -258,7 +283,6 @@ bool launch_batch(rmq_server* s, Slot& sl, std::unique_lock<std::mutex>& lk) {
             continue;
         }
         if (nq + r.q > max_q) break;
-        sl.req_off.push_back(nq);
         sl.reqs.push_back(*it);
         sl.rptr.push_back(&r);
         nq += r.q;
@@ -280,11 +304,13 @@ bool launch_batch(rmq_server* s, Slot& sl, std::unique_lock<std::mutex>& lk) {
     if (inject) s->fail_batches--;
     lk.unlock();
 
-    // Upload: descriptors | q_off[nr + 1] | unit_off[nr + 1] | queries.
+    // Upload: descriptors | q_off[nr + 1] | unit_off[nr + 1] | io[nr] |
+    // owner of each unit | the staged requests' queries.
     const size_t hdr = header_bytes(nr);
     rmq::ArrayDesc* hd = reinterpret_cast<rmq::ArrayDesc*>(sl.h_in);
     uint64_t* hq = reinterpret_cast<uint64_t*>(sl.h_in + size_t(nr) * sizeof(rmq::ArrayDesc));
     uint64_t* hu = hq + (nr + 1);
+    rmq::ServeIO* hio = reinterpret_cast<rmq::ServeIO*>(hu + (nr + 1));
     std::memcpy(hd, descs.data(), nr * sizeof(rmq::ArrayDesc));
     hq[0] = 0;
     hu[0] = 0;
@@ -295,23 +321,43 @@ bool launch_batch(rmq_server* s, Slot& sl, std::unique_lock<std::mutex>& lk) {
     uint32_t* h_owner = reinterpret_cast<uint32_t*>(sl.h_in + hdr);
     const size_t qat = hdr + owner_bytes(hu[nr]);
     uint32_t* h_q = reinterpret_cast<uint32_t*>(sl.h_in + qat);
+    // staged requests' queries and results are packed in request order
+    uint64_t snq = 0;
+    sl.req_off.assign(nr, 0);
+    for (uint32_t i = 0; i < nr; ++i) {
+        if (!reqs[i]->direct) {
+            sl.req_off[i] = snq;
+            snq += reqs[i]->q;
+        }
+    }
+    const size_t bb = bad_bytes(nr);
+    uint32_t* d_idx = reinterpret_cast<uint32_t*>(sl.d_out + bb);
+    float* d_min = reinterpret_cast<float*>(sl.d_out + bb + snq * sizeof(uint32_t));
     for (uint32_t i = 0; i < nr; ++i) {
         for (uint64_t u = hu[i]; u < hu[i + 1]; ++u) h_owner[u] = i;
-        std::memcpy(h_q + 2 * sl.req_off[i], reqs[i]->h_lr, reqs[i]->q * 2 * sizeof(uint32_t));
+        const Request& r = *reqs[i];
+        if (r.direct) {
+            hio[i] = rmq::ServeIO{reinterpret_cast<const uint2*>(r.d_lr), r.d_idx, r.d_min};
+        } else {
+            const uint64_t o = sl.req_off[i];
+            std::memcpy(h_q + 2 * o, r.h_lr, r.q * 2 * sizeof(uint32_t));
+            hio[i] = rmq::ServeIO{reinterpret_cast<const uint2*>(sl.d_in + qat) + o,
+                                  r.h_idx != nullptr ? d_idx + o : nullptr, r.h_min != nullptr ? d_min + o : nullptr};
+        }
     }
     const rmq::ArrayDesc* dd = reinterpret_cast<const rmq::ArrayDesc*>(sl.d_in);
     const uint64_t* dq = reinterpret_cast<const uint64_t*>(sl.d_in + size_t(nr) * sizeof(rmq::ArrayDesc));
     const uint64_t* du = dq + (nr + 1);
-    sl.nq = nq;
-    uint32_t* d_idx = reinterpret_cast<uint32_t*>(sl.d_out);
-    float* d_min = reinterpret_cast<float*>(sl.d_out + nq * sizeof(uint32_t));
+    sl.snq = snq;
+    sl.nr = nr;
     // An injected failure (rmq_server_fail_next_batches) stands in for a
     // failing upload: nothing is issued and the batch takes the error path.
     cudaError_t e = inject ? cudaErrorInvalidConfiguration
-                           : cudaMemcpyAsync(sl.d_in, sl.h_in, qat + nq * 2 * sizeof(uint32_t),
+                           : cudaMemcpyAsync(sl.d_in, sl.h_in, qat + snq * 2 * sizeof(uint32_t),
                                              cudaMemcpyHostToDevice, sl.stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(sl.d_out, 0, bb, sl.stream);
     if (e == cudaSuccess) {
-        rmq::BatchQueryArgs a;
+        rmq::ServeQueryArgs a;
         a.values = reinterpret_cast<const float*>(s->arena);
         a.descs = dd;
         a.owner = reinterpret_cast<const uint32_t*>(sl.d_in + hdr);
@@ -320,13 +366,12 @@ bool launch_batch(rmq_server* s, Slot& sl, std::unique_lock<std::mutex>& lk) {
         a.total_units = hu[nr];
         a.lvl_val = reinterpret_cast<const float*>(s->arena);
         a.lvl_idx = reinterpret_cast<const uint32_t*>(s->arena);
-        a.qs = reinterpret_cast<const uint2*>(sl.d_in + qat);
-        a.out_min = d_min;
-        a.out_idx = d_idx;
+        a.io = reinterpret_cast<const rmq::ServeIO*>(du + (nr + 1));
+        a.bad = reinterpret_cast<uint32_t*>(sl.d_out);
         a.threads = s->cfg.query_threads;
-        e = rmq::launch_batch_query(a, sl.stream);
+        e = rmq::launch_serve_query(a, sl.stream);
     }
-    if (e == cudaSuccess) e = cudaMemcpyAsync(sl.h_out, sl.d_out, nq * 8, cudaMemcpyDeviceToHost, sl.stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(sl.h_out, sl.d_out, bb + snq * 8, cudaMemcpyDeviceToHost, sl.stream);
     if (e == cudaSuccess) e = cudaEventRecord(sl.done, sl.stream);
     if (e != cudaSuccess) {
         // Launch failure: the batch's requests complete with RMQ_ERR_CUDA.
@@ -468,10 +513,11 @@ int rmq_server_create(const rmq_server_config* cfg_in, rmq_server** out) {
         if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming);
         const size_t in_bytes = header_bytes(mr) + owner_bytes(mq / 32 + mr) + mq * 2 * sizeof(uint32_t);
+        const size_t out_bytes = bad_bytes(mr) + mq * 8;
         if (e == cudaSuccess) e = cudaMallocHost(&sl.h_in, in_bytes);
-        if (e == cudaSuccess) e = cudaMallocHost(&sl.h_out, mq * 8);
+        if (e == cudaSuccess) e = cudaMallocHost(&sl.h_out, out_bytes);
         if (e == cudaSuccess) e = cudaMalloc(&sl.d_in, in_bytes);
-        if (e == cudaSuccess) e = cudaMalloc(&sl.d_out, mq * 8);
+        if (e == cudaSuccess) e = cudaMalloc(&sl.d_out, out_bytes);
     }
     if (e != cudaSuccess) {
         cudaGetLastError();
@@ -496,14 +542,22 @@ int rmq_server_submit(rmq_server* s, uint64_t array_id, const uint32_t* h_lr, ui
                       float* h_min, uint64_t* request_id) {
     if (s == nullptr || request_id == nullptr || (h_argmin == nullptr && h_min == nullptr)) return RMQ_ERR_ARG;
     if (q == 0 || h_lr == nullptr || q > s->cfg.max_batch_queries) return RMQ_ERR_ARG;
-    std::lock_guard<std::mutex> lock(s->mu);
-    if (array_id >= s->arrays.size() || s->stop) return RMQ_ERR_ARG;
     Request r;
     r.array = array_id;
     r.h_lr = h_lr;
     r.q = q;
     r.h_idx = h_argmin;
     r.h_min = h_min;
+    // Page-locked, mapped request buffers are read and written in place by
+    // the kernel (no staging copies); anything else is staged.
+    r.d_lr = static_cast<const uint32_t*>(mapped_range(h_lr, q * 2 * sizeof(uint32_t), 8));
+    r.d_idx = static_cast<uint32_t*>(mapped_range(h_argmin, q * sizeof(uint32_t), 4));
+    r.d_min = static_cast<float*>(mapped_range(h_min, q * sizeof(float), 4));
+    r.direct = r.d_lr != nullptr && (h_argmin == nullptr || r.d_idx != nullptr) &&
+               (h_min == nullptr || r.d_min != nullptr);
+    std::lock_guard<std::mutex> lock(s->mu);
+    if (array_id >= s->arrays.size() || s->stop) return RMQ_ERR_ARG;
+    if (r.direct) s->stats.direct_requests++;
     r.t_submit = Clock::now();
     *request_id = s->next_request++;
     s->requests.emplace(*request_id, r);

@@ -401,6 +401,8 @@ class BatchInfo(ctypes.Structure):
         ("total_queries", ctypes.c_uint64),
         ("build_ms", ctypes.c_float),
         ("query_ms", ctypes.c_float),
+        ("class_threshold", ctypes.c_uint64 * 3),
+        ("class_upper", ctypes.c_uint64 * 3),
     ]
 
 
@@ -419,6 +421,7 @@ def _bind_batch() -> ctypes.CDLL:
         L.rmq_batch_autotune.argtypes = [_P, _P, ctypes.POINTER(BatchInfo)]
         L.rmq_batch_get_info.argtypes = [_P, ctypes.POINTER(BatchInfo)]
         L.rmq_batch_set_tuning.argtypes = [_P, _U64, ctypes.c_uint32, _P]
+        L.rmq_batch_set_class_tuning.argtypes = [_P, _P, ctypes.c_uint32, _P]
         L.rmq_batch_destroy.argtypes = [_P]
         L.rmq_batch_destroy.restype = None
         L.rmq_gen_values_device.argtypes = [_P, _U64, _U64, _P]
@@ -483,6 +486,14 @@ class Batch:
         if st != RMQ_OK:
             raise RMQError(st, "rmq_batch_set_tuning")
 
+    def set_class_tuning(self, class_thresholds, query_block: int, stream=None) -> None:
+        """Applies one t per array-size class (three values, as
+        BatchInfo.class_threshold reports them); rebuild before querying."""
+        arr = (ctypes.c_uint64 * 3)(*[int(x) for x in class_thresholds])
+        st = _bind_batch().rmq_batch_set_class_tuning(self._h, arr, int(query_block), _stream_handle(stream))
+        if st != RMQ_OK:
+            raise RMQError(st, "rmq_batch_set_class_tuning")
+
     def workload_key(self) -> str:
         """Identifies the tuning problem: the GPU, the array sizes and the
         per-array query counts (the autotuner times exactly these)."""
@@ -505,7 +516,10 @@ class Batch:
             table = json.loads(Path(cache).read_text())
             hit = table.get(key)
             if hit is not None:
-                self.set_tuning(hit["scan_threshold"], hit["query_block"], stream)
+                if "class_threshold" in hit:
+                    self.set_class_tuning(hit["class_threshold"], hit["query_block"], stream)
+                else:
+                    self.set_tuning(hit["scan_threshold"], hit["query_block"], stream)
                 self.build(stream)
                 return self.info()
         info = BatchInfo()
@@ -514,6 +528,7 @@ class Batch:
             raise RMQError(st, "rmq_batch_autotune")
         if cache is not None:
             table[key] = {"scan_threshold": int(info.scan_threshold), "query_block": int(info.query_block),
+                          "class_threshold": [int(x) for x in info.class_threshold],
                           "query_ms": float(info.query_ms), "arrays": self.num_arrays}
             Path(cache).write_text(json.dumps(table, indent=1, sort_keys=True))
         return info
@@ -589,7 +604,8 @@ class ServerConfig(ctypes.Structure):
 class ServerStats(ctypes.Structure):
     _fields_ = [(name, ctypes.c_uint64) for name in (
         "requests_done", "queries_done", "batches", "registrations", "evictions", "readmissions",
-        "resident_arrays", "resident_bytes", "max_requests_per_batch", "max_batches_in_flight")]
+        "resident_arrays", "resident_bytes", "max_requests_per_batch", "max_batches_in_flight",
+        "direct_requests")]
 
     def as_dict(self) -> dict:
         return {name: int(getattr(self, name)) for name, _ in self._fields_}

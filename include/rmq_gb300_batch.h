@@ -33,6 +33,8 @@ typedef struct {
     uint64_t total_queries;     /* of the last rmq_batch_set_queries                         */
     float    build_ms;          /* device time of the last rmq_batch_build (CUDA events)    */
     float    query_ms;          /* device time of the last timed query pass (autotune)      */
+    uint64_t class_threshold[3];  /* t of each array-size class (scan_threshold = the last)  */
+    uint64_t class_upper[3];      /* class c holds the arrays with class_upper[c-1] <= n < class_upper[c] */
 } rmq_batch_info;
 
 /* Creates a batch over num_arrays arrays packed in d_values: array a is
@@ -74,9 +76,12 @@ int rmq_batch_run(rmq_batch* b, rmq_stream_t stream);
 int rmq_batch_run_per_array(rmq_batch* b, rmq_stream_t stream);
 
 /* Autotuner: times the query kernel on the registered queries for each
- * candidate scan threshold t in {16, 32, 64, 256, 1024} and CTA size in
- * {64, 128, 256, 512} threads, keeps the fastest and rebuilds with it.
- * Blocking.  The choice is reported in *info (may be NULL). */
+ * candidate scan threshold t in {16, 32, 64, 256, 1024} (the same for every
+ * array) and CTA size in {64, 128, 256, 512} threads; then, keeping the best
+ * CTA size, tries each t for each array-size class in turn (arrays below 2^14
+ * entries, below 2^18, and the rest; the largest class first) and keeps a
+ * class's new t when it is faster by more than 0.5 %.  Rebuilds with the
+ * choice.  Blocking.  The choice is reported in *info (may be NULL). */
 int rmq_batch_autotune(rmq_batch* b, rmq_stream_t stream, rmq_batch_info* info);
 
 /* Applies a known choice (for example one rmq_batch_autotune made earlier for
@@ -85,6 +90,12 @@ int rmq_batch_autotune(rmq_batch* b, rmq_stream_t stream, rmq_batch_info* info);
  * rmq_batch_run) before querying.  RMQ_ERR_UNSUPPORTED when t would need more
  * level storage than the batch holds (any t >= 16, or the creation t, fits). */
 int rmq_batch_set_tuning(rmq_batch* b, uint64_t scan_threshold, uint32_t query_block, rmq_stream_t stream);
+
+/* The same with one t per array-size class (class_thresholds[3], each >= 8,
+ * in the order of rmq_batch_info.class_upper), as rmq_batch_autotune
+ * reports it. */
+int rmq_batch_set_class_tuning(rmq_batch* b, const uint64_t* class_thresholds, uint32_t query_block,
+                               rmq_stream_t stream);
 
 int rmq_batch_get_info(const rmq_batch* b, rmq_batch_info* info);
 

@@ -40,6 +40,7 @@ typedef struct {
     uint64_t resident_bytes;
     uint64_t max_requests_per_batch;
     uint64_t max_batches_in_flight;
+    uint64_t direct_requests;  /* requests whose page-locked buffers the kernel read and wrote in place */
 } rmq_server_stats;
 
 /* One event of a recorded request stream (rmq_server_replay). */
@@ -74,7 +75,11 @@ int rmq_server_register_host(rmq_server* s, const float* h_values, uint64_t n, u
 /* Submits q inclusive queries (h_lr[2i] = l, h_lr[2i+1] = r) on array_id.
  * The server writes the argmin and / or minimum of each query into h_argmin
  * / h_min (either may be NULL, not both); the buffers must stay valid until
- * the request is done.  Non-blocking. */
+ * the request is done.  Non-blocking.  When every buffer given is
+ * page-locked and mapped (cudaHostAlloc, cudaHostRegister; h_lr 8-byte and
+ * the results 4-byte aligned), the batch's kernel reads the queries and
+ * writes the results in place over the CPU-GPU link; otherwise the server
+ * copies them through its pinned staging buffers. */
 int rmq_server_submit(rmq_server* s, uint64_t array_id, const uint32_t* h_lr, uint64_t q, uint32_t* h_argmin,
                       float* h_min, uint64_t* request_id);
 

@@ -207,3 +207,42 @@ def test_per_array_loop_matches_batched(cuda):
         b.run()
         torch.cuda.synchronize()
         _check(out_min, out_idx, emin, eidx, "graph after the loop")
+
+
+def test_class_thresholds(cuda):
+    """One scan threshold per array-size class: any combination gives exact
+    results, and the autotuner reports a valid choice per class."""
+    import torch
+    rng = np.random.default_rng(21)
+    sizes = [int(x) for x in np.exp(rng.uniform(np.log(1 << 10), np.log(1 << 20), 30))] + [100, 20_000, 300_000]
+    dv, dq, offs, arrays, qs, qo = _make_batch(cuda, sizes, 21)
+    emin, eidx = _expected(arrays, qs, qo)
+    q = qs.shape[0]
+    out_min = torch.empty(q, dtype=torch.float32, device=cuda)
+    out_idx = torch.empty(q, dtype=torch.int32, device=cuda)
+    with R.Batch(dv, offs, sizes, t=64) as b:
+        b.set_queries(dq, qo, out_idx, out_min)
+        for tc in ([16, 256, 1024], [1024, 16, 32], [64, 64, 16]):
+            b.set_class_tuning(tc, 128)
+            info = b.info()
+            assert list(info.class_threshold) == tc and info.scan_threshold == tc[2]
+            out_min.fill_(-1)
+            out_idx.fill_(-1)
+            b.run()
+            torch.cuda.synchronize()
+            _check(out_min, out_idx, emin, eidx, f"class thresholds {tc}")
+            out_min.fill_(-1)
+            out_idx.fill_(-1)
+            b.run_per_array()
+            torch.cuda.synchronize()
+            _check(out_min, out_idx, emin, eidx, f"per-array loop, class thresholds {tc}")
+        with pytest.raises(R.RMQError):
+            b.set_class_tuning([4, 64, 64], 128)
+        info = b.autotune()
+        assert all(t in (16, 32, 64, 256, 1024) for t in info.class_threshold)
+        assert list(info.class_upper)[:2] == [1 << 14, 1 << 18]
+        out_min.fill_(-1)
+        out_idx.fill_(-1)
+        b.run()
+        torch.cuda.synchronize()
+        _check(out_min, out_idx, emin, eidx, "after the per-class autotune")

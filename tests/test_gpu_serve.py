@@ -155,3 +155,60 @@ def test_serial_loop_comparator_matches_oracle(cuda):
             assert gm[o:o + q].tobytes() == oracle.rmq_min(arrays[aid], lr[o:o + q]).tobytes()
     for h in hs:
         h.close()
+
+
+def test_page_locked_requests_are_answered_in_place(cuda):
+    """Requests whose buffers are page-locked are read and written in place by
+    the batch kernel (no staging); mixed in one batch with staged requests,
+    every result equals the oracle's, minima-only and argmin-only requests
+    included, and invalid queries are reported per request."""
+    import torch
+    rng = np.random.default_rng(13)
+    sizes = [3000, 1 << 17, 70_001]
+    arrays = [(rng.integers(0, 60, n) / 9).astype(np.float32) for n in sizes]  # ties
+    with R.Server(hbm_budget_bytes=256 << 20, slots=3) as srv:
+        ids = [srv.register_host(a) for a in arrays]
+        for aid in ids:  # every array built before the mix
+            w = np.zeros((1, 2), np.uint32)
+            assert srv.wait(srv.submit(aid, w, np.empty(1, np.uint32), None))[0] == R.RMQ_OK
+        prepared = []
+        for i in range(60):
+            aid = int(rng.integers(0, len(sizes)))
+            qs = _queries(rng, sizes[aid], int(rng.integers(1, 4000)))
+            pinned = i % 3 != 0
+            bad = i % 11 == 5
+            if bad:
+                qs[0] = (7, 3)  # l > r
+            if pinned:
+                t_q = torch.from_numpy(qs.view(np.int32).reshape(-1)).pin_memory()
+                lr = t_q.numpy().view(np.uint32).reshape(-1, 2)
+                oi_t = torch.zeros(qs.shape[0], dtype=torch.int32).pin_memory()
+                om_t = torch.zeros(qs.shape[0], dtype=torch.float32).pin_memory()
+                keep = (t_q, oi_t, om_t)
+                oi = oi_t.numpy().view(np.uint32)
+                om = om_t.numpy()
+            else:
+                lr, oi, om, keep = qs, np.zeros(qs.shape[0], np.uint32), np.zeros(qs.shape[0], np.float32), None
+            which = i % 4  # 0: both outputs, 1: argmin only, 2: minima only, 3: both
+            prepared.append((aid, qs, lr, oi, om, which, bad, keep, pinned))
+        # all buffers ready first: the submissions then arrive close together
+        reqs = [(srv.submit(aid, lr, oi if which != 2 else None, om if which != 1 else None),
+                 aid, qs, oi, om, which, bad, keep)
+                for aid, qs, lr, oi, om, which, bad, keep, _ in prepared]
+        for rid, aid, qs, oi, om, which, bad, keep in reqs:
+            st, _ = srv.wait(rid)
+            assert st == (R.RMQ_ERR_QUERY_RANGE if bad else R.RMQ_OK)
+            ok = np.ones(qs.shape[0], bool)
+            if bad:
+                ok[0] = False
+                if which != 2:
+                    assert oi[0] == R.NO_POS
+                if which != 1:
+                    assert np.isnan(om[0])
+            if which != 2:
+                assert np.array_equal(oi[ok], oracle.rmq_argmin(arrays[aid], qs[ok]))
+            if which != 1:
+                assert om[ok].tobytes() == oracle.rmq_min(arrays[aid], qs[ok]).tobytes()
+        stats = srv.stats()
+    # exactly the requests with page-locked buffers were answered in place
+    assert stats["direct_requests"] == sum(1 for x in prepared if x[-1])
