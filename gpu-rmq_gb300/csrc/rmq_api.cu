@@ -99,14 +99,20 @@ int resolve_config(uint64_t n, const rmq_config* cfg_in, int* variant, int* rf_l
     else rmq_config_init(&cfg);
     int v = cfg.variant;
     if (v == RMQ_VARIANT_AUTO) v = RMQ_VARIANT_VL;
-    if (v != RMQ_VARIANT_CL && v != RMQ_VARIANT_VL) return RMQ_ERR_ARG;
-    int r = cfg.rf_log != 0 ? cfg.rf_log : (v == RMQ_VARIANT_CL ? kClRfLog : kVlRfLog);
+    // CL and its three ablated work distributions share the CL preconditions.
+    const bool cl = v == RMQ_VARIANT_CL || v == RMQ_VARIANT_CL_NO_SHUFFLE || v == RMQ_VARIANT_CL_QUERY_PER_TILE ||
+                    v == RMQ_VARIANT_CL_ATOMIC;
+    if (!cl && v != RMQ_VARIANT_VL) return RMQ_ERR_ARG;
+    int r = cfg.rf_log != 0 ? cfg.rf_log : (cl ? kClRfLog : kVlRfLog);
     if (r < 3 || r > 5) return RMQ_ERR_ARG;
-    uint64_t tt = cfg.scan_threshold != 0 ? cfg.scan_threshold : (v == RMQ_VARIANT_CL ? kClT : kVlT);
+    uint64_t tt = cfg.scan_threshold != 0 ? cfg.scan_threshold : (cl ? kClT : kVlT);
     const uint64_t rf = uint64_t(1) << r;
     // The reference's own preconditions (src/xxx.h:211, src/xxx.h:938).
-    if (v == RMQ_VARIANT_CL && tt < 2 * rf) return RMQ_ERR_ARG;
+    if (cl && tt < 2 * rf) return RMQ_ERR_ARG;
     if (v == RMQ_VARIANT_VL && tt < rf) return RMQ_ERR_ARG;
+    // The atomic combine orders a lane's candidates inside a query with 24
+    // bits of sector number: pieces of at most 2^27 entries.
+    if (v == RMQ_VARIANT_CL_ATOMIC && tt >= (uint64_t(1) << 27)) return RMQ_ERR_UNSUPPORTED;
     int g = cfg.lanes != 0 ? cfg.lanes : kClLanes;
     if (g != 2 && g != 4 && g != 8 && g != 16 && g != 32) return RMQ_ERR_ARG;
     (void)n;

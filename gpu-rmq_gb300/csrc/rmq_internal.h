@@ -47,7 +47,7 @@ struct QueryArgs {
     const uint64_t* qs64;
     uint64_t* out_idx64;
     uint32_t* err;       // invalid-query counter or null
-    int variant;         // 1 = CL, 2 = VL
+    int variant;         // rmq_variant: 1 = CL, 2 = VL, 3 / 4 / 5 = CL without shuffles / a tile per query / atomic combine
     int lanes;           // CL tile width
     uint32_t rf_log;
     const void* persist_base;   // L2 access-policy window (null = none)

@@ -110,30 +110,139 @@ __device__ __forceinline__ void cl_query(const Levels& lv, uint32_t l, uint32_t 
     cl_pair<G, ARGMIN>(lv, k, l, r, kGroupFinal, 0u, 0u, 0u, lane, pol, b);
 }
 
-template <int R, int G, bool ARGMIN>
+// Work distributions of the CL kernel (rmq_variant): the reference's alg 16
+// (a tile answers its G queries one after another, each broadcast to the
+// tile by shuffles, src/xxx.h:124-200) and its three ablations:
+//   kClNoShuffle     alg 23 (src/xxx.h:302-369): every lane loads the query
+//                    of the current turn itself, no ballot or broadcast;
+//   kClQueryPerTile  alg 24 (src/xxx.h:470-528): one query per tile, q x G
+//                    threads, no turns;
+//   kClAtomic        alg 19 (src/xxx.h:631-686): as alg 23, but the lanes
+//                    combine their candidates with atomic minima (here on a
+//                    64-bit (value, position) key in shared memory) instead
+//                    of a shuffle reduction.
+// All four give the same results (the reference's alg 24 indexes its output
+// by tile in a grid-stride loop and alg 23 reads past q; here every query is
+// answered exactly once and nothing is read past q).
+constexpr int kClShuffle = 0, kClNoShuffle = 1, kClQueryPerTile = 2, kClAtomic = 3;
+
+// First entry equal to b.v inside lane candidate b's sector: its value bits
+// and its level-0 position (for a coarse level, the stored index; only when
+// WANT_POS).
+template <bool WANT_POS>
+__device__ __forceinline__ void cl_locate(const Levels& lv, const LaneBest& b, float m, const L2Policies& pol,
+                                          float& val, uint32_t& pos, bool& pos_ok) {
+    const uint32_t k = b.meta & 0xffu;
+    const uint32_t jlo = (b.meta >> 8) & 0xffu;
+    const uint32_t jhi = (b.meta >> 16) & 0xffu;
+    float v[8];
+    load_level_sector<uint32_t, false>(lv, k, b.s, pol, v);
+    uint32_t jj = jlo;
+#pragma unroll
+    for (int t = 7; t >= 0; --t)
+        if (uint32_t(t) >= jlo && uint32_t(t) < jhi && v[t] == m) jj = uint32_t(t);
+    val = v[0];
+#pragma unroll
+    for (int t = 1; t < 8; ++t) val = (uint32_t(t) == jj) ? v[t] : val;
+    const uint32_t e = b.s + jj;
+    pos_ok = true;
+    pos = e;
+    if (WANT_POS && k > 0) {
+#if RMQ_DEBUG_BOUNDS
+        pos_ok = bounds_ok(lv.idx[k] != nullptr && e < lv.size[k]);
+        if (!pos_ok) return;
+#endif
+        pos = ld_index(lv.idx[k] + e);
+    }
+}
+
+template <int R, int G, bool ARGMIN, int MODE>
 __global__ void __launch_bounds__(256)
 query_cl_kernel(Levels lv, const uint2* __restrict__ qs, uint32_t q, float* __restrict__ out_min,
                 uint32_t* __restrict__ out_idx, uint32_t* __restrict__ err) {
-    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint64_t gtid = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    const uint32_t tid = uint32_t(gtid);
     const uint32_t lane = threadIdx.x & (G - 1u);
     const uint32_t wl = threadIdx.x & 31u;
     const uint32_t mask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (wl - lane));
-    const uint32_t base = tid - lane;  // first query of the tile
+    // The tile's queries: base .. base + G - 1 (one per turn), or the single
+    // query gtid / G for kClQueryPerTile.
+    const uint64_t base = MODE == kClQueryPerTile ? gtid / G : uint64_t(tid - lane);
+    constexpr uint32_t kTurns = MODE == kClQueryPerTile ? 1u : uint32_t(G);
+    __shared__ unsigned long long slot[MODE == kClAtomic ? 256 / G : 1];
     const L2Policies pol = make_policies();
 
+    uint32_t vmask = 0;
     uint2 Q = make_uint2(1u, 0u);
-    if (tid < q) Q = ld_query(qs + tid);
-    const bool valid = tid < q && Q.x <= Q.y && Q.y < lv.size[0];
-    if (tid < q && !valid) {
-        if (out_min != nullptr) st_stream(out_min + tid, f_nan());
-        if (ARGMIN) st_stream(out_idx + tid, kNoPos);
-        if (err != nullptr) atomicAdd(err, 1u);
+    if constexpr (MODE == kClShuffle) {
+        if (tid < q) Q = ld_query(qs + tid);
+        const bool valid = tid < q && Q.x <= Q.y && Q.y < lv.size[0];
+        if (tid < q && !valid) {
+            if (out_min != nullptr) st_stream(out_min + tid, f_nan());
+            if (ARGMIN) st_stream(out_idx + tid, kNoPos);
+            if (err != nullptr) atomicAdd(err, 1u);
+        }
+        vmask = __ballot_sync(mask, valid) >> (wl - lane);  // the tile's valid queries
     }
-    const uint32_t vmask = __ballot_sync(mask, valid) >> (wl - lane);  // the tile's valid queries
-    for (uint32_t j = 0; j < G; ++j) {
-        if (((vmask >> j) & 1u) == 0u) continue;  // uniform across the tile
-        const uint32_t l = __shfl_sync(mask, Q.x, j, G);
-        const uint32_t r = __shfl_sync(mask, Q.y, j, G) + 1u;
+    for (uint32_t j = 0; j < kTurns; ++j) {
+        const uint64_t qi = base + j;                             // query of this turn
+        const uint32_t owner = MODE == kClQueryPerTile ? 0u : j;  // the lane that stores its answer
+        uint32_t l, r;
+        if constexpr (MODE == kClShuffle) {
+            if (((vmask >> j) & 1u) == 0u) continue;  // uniform across the tile
+            l = __shfl_sync(mask, Q.x, j, G);
+            r = __shfl_sync(mask, Q.y, j, G) + 1u;
+        } else {
+            if (qi >= q) break;  // uniform across the tile
+            const uint2 Qj = ld_query(qs + qi);  // the same address on every lane
+            if (!(Qj.x <= Qj.y && Qj.y < lv.size[0])) {
+                if (lane == owner) {
+                    if (out_min != nullptr) st_stream(out_min + qi, f_nan());
+                    if (ARGMIN) st_stream(out_idx + qi, kNoPos);
+                    if (err != nullptr) atomicAdd(err, 1u);
+                }
+                continue;
+            }
+            l = Qj.x;
+            r = Qj.y + 1u;
+        }
+        if constexpr (MODE == kClAtomic) {
+            // Every lane's candidate is its first entry equal to its minimum;
+            // the tile keeps the least (value, position order) with atomicMin
+            // on a 64-bit key and the lane holding it stores the answer.  The
+            // value key puts -0.0 and +0.0 together, so ties among zeros go to
+            // the first, whose bits are stored.
+            LaneBest b{f_inf(), kKeyNone, 0u, 0u};
+            cl_query<R, G, true>(lv, l, r, lane, pol, b);
+            unsigned long long key = ~0ull;
+            if (b.key != kKeyNone) {
+                // position order inside the query: group (8 bits), sector of the piece (24 bits)
+                const uint32_t order = (uint32_t(b.key >> 32) << 24) | uint32_t(b.key & 0xffffffu);
+                key = (uint64_t(min_key(b.v)) << 32) | order;
+            }
+            if (lane == owner) slot[threadIdx.x / G] = ~0ull;
+            __syncwarp(mask);
+            if (key != ~0ull) atomicMin(&slot[threadIdx.x / G], key);
+            __syncwarp(mask);
+            const unsigned long long win = *reinterpret_cast<volatile unsigned long long*>(&slot[threadIdx.x / G]);
+            if (win == ~0ull) {
+                // no candidate compared at all: NaN inputs only (outside the
+                // contract); the scan's answer is the first entry
+                if (lane == owner) {
+                    if (ARGMIN) st_stream(out_idx + qi, l);
+                    if (out_min != nullptr) st_stream(out_min + qi, __ldg(lv.val[0] + l));
+                }
+            } else if (key == win) {
+                float val;
+                uint32_t pos;
+                bool pos_ok;
+                cl_locate<ARGMIN>(lv, b, b.v, pol, val, pos, pos_ok);
+                if (ARGMIN && pos_ok) st_stream(out_idx + qi, pos);
+                if (out_min != nullptr) st_stream(out_min + qi, val);
+            }
+            __syncwarp(mask);  // the slot is reused by the next turn
+            continue;
+        }
         LaneBest b{f_inf(), kKeyNone, 0u, 0u};
         cl_query<R, G, ARGMIN>(lv, l, r, lane, pol, b);
         float m = b.v;
@@ -144,7 +253,7 @@ query_cl_kernel(Levels lv, const uint2* __restrict__ qs, uint32_t q, float* __re
             // A +0.0 minimum means no -0.0 in the range (min.f32 returns -0.0
             // whenever one meets a zero): only -0.0 needs the first zero's bits.
             if (__float_as_uint(m) != 0x80000000u) {
-                if (lane == j) st_stream(out_min + base + j, m);
+                if (lane == owner) st_stream(out_min + qi, m);
                 continue;
             }
             // A -0.0 minimum: locate the first zero for its bits.
@@ -162,32 +271,17 @@ query_cl_kernel(Levels lv, const uint2* __restrict__ qs, uint32_t q, float* __re
             if (key == kKeyNone) {
                 // No entry compared equal to the minimum: NaN inputs only
                 // (outside the contract); the scan's answer is the first entry.
-                if (lane == j) {
-                    if (out_idx != nullptr) st_stream(out_idx + base + j, l);
-                    if (out_min != nullptr) st_stream(out_min + base + j, __ldg(lv.val[0] + l));
+                if (lane == owner) {
+                    if (out_idx != nullptr) st_stream(out_idx + qi, l);
+                    if (out_min != nullptr) st_stream(out_min + qi, __ldg(lv.val[0] + l));
                 }
             } else if (b.key == key && b.v == m) {
-                const uint32_t k = b.meta & 0xffu;
-                const uint32_t jlo = (b.meta >> 8) & 0xffu;
-                const uint32_t jhi = (b.meta >> 16) & 0xffu;
-                float v[8];
-                load_level_sector<uint32_t, false>(lv, k, b.s, pol, v);
-                uint32_t jj = jlo;
-#pragma unroll
-                for (int t = 7; t >= 0; --t)
-                    if (uint32_t(t) >= jlo && uint32_t(t) < jhi && v[t] == m) jj = uint32_t(t);
-                float val = v[0];
-#pragma unroll
-                for (int t = 1; t < 8; ++t) val = (uint32_t(t) == jj) ? v[t] : val;
-                const uint32_t e = b.s + jj;
-#if RMQ_DEBUG_BOUNDS
-                const bool idx_ok = out_idx == nullptr || k == 0 || bounds_ok(lv.idx[k] != nullptr && e < lv.size[k]);
-#else
-                constexpr bool idx_ok = true;
-#endif
-                if (out_idx != nullptr && idx_ok)
-                    st_stream(out_idx + base + j, k == 0 ? e : ld_index(lv.idx[k] + e));
-                if (out_min != nullptr) st_stream(out_min + base + j, val);
+                float val;
+                uint32_t pos;
+                bool pos_ok;
+                cl_locate<ARGMIN>(lv, b, m, pol, val, pos, pos_ok);
+                if (out_idx != nullptr && pos_ok) st_stream(out_idx + qi, pos);
+                if (out_min != nullptr) st_stream(out_min + qi, val);
             }
         }
     }
@@ -283,6 +377,24 @@ static cudaError_t launch_with_window(K kernel, uint32_t grid, uint32_t block, c
 // +2.1 %.  64-thread blocks: within 1 % of these, uniform lengths -1 %.
 constexpr uint32_t kQueryBlock = 128;
 
+template <int R, int MODE>
+static cudaError_t launch_cl(const QueryArgs& a, cudaStream_t s, uint32_t grid, uint32_t q32, bool argmin) {
+#define RMQ_CL(G)                                                                                                \
+    return argmin ? launch_with_window(query_cl_kernel<R, G, true, MODE>, grid, kQueryBlock, a, s, a.lv, a.qs,  \
+                                         q32, a.out_min, a.out_idx, a.err)                                        \
+                  : launch_with_window(query_cl_kernel<R, G, false, MODE>, grid, kQueryBlock, a, s, a.lv, a.qs, \
+                                         q32, a.out_min, static_cast<uint32_t*>(nullptr), a.err)
+    switch (a.lanes) {
+        case 2: RMQ_CL(2);
+        case 4: RMQ_CL(4);
+        case 8: RMQ_CL(8);
+        case 16: RMQ_CL(16);
+        case 32: RMQ_CL(32);
+        default: return cudaErrorInvalidValue;
+    }
+#undef RMQ_CL
+}
+
 template <int R>
 static cudaError_t launch_query_r(const QueryArgs& a, cudaStream_t s) {
     const bool argmin = a.out_idx != nullptr || a.out_idx64 != nullptr;
@@ -303,20 +415,19 @@ static cudaError_t launch_query_r(const QueryArgs& a, cudaStream_t s) {
                                              a.qs, a.q, a.out_min, static_cast<uint32_t*>(nullptr), a.err);
     }
     const uint32_t q32 = uint32_t(a.q);
-#define RMQ_CL(G)                                                                                               \
-    return argmin ? launch_with_window(query_cl_kernel<R, G, true>, grid, kQueryBlock, a, s, a.lv, a.qs, q32,  \
-                                         a.out_min, a.out_idx, a.err)                                            \
-                  : launch_with_window(query_cl_kernel<R, G, false>, grid, kQueryBlock, a, s, a.lv, a.qs, q32, \
-                                         a.out_min, static_cast<uint32_t*>(nullptr), a.err)
-    switch (a.lanes) {
-        case 2: RMQ_CL(2);
-        case 4: RMQ_CL(4);
-        case 8: RMQ_CL(8);
-        case 16: RMQ_CL(16);
-        case 32: RMQ_CL(32);
+    switch (a.variant) {
+        case 1: return launch_cl<R, kClShuffle>(a, s, grid, q32, argmin);
+        case 3: return launch_cl<R, kClNoShuffle>(a, s, grid, q32, argmin);
+        case 4: {
+            // one tile of `lanes` threads per query
+            const uint64_t threads = a.q * uint64_t(a.lanes);
+            const uint64_t g = (threads + kQueryBlock - 1u) / kQueryBlock;
+            if (g > 0x7FFFFFFFull) return cudaErrorInvalidConfiguration;
+            return launch_cl<R, kClQueryPerTile>(a, s, uint32_t(g), q32, argmin);
+        }
+        case 5: return launch_cl<R, kClAtomic>(a, s, grid, q32, argmin);
         default: return cudaErrorInvalidValue;
     }
-#undef RMQ_CL
 }
 
 #if RMQ_DEBUG_BOUNDS

@@ -18,7 +18,8 @@
 //    22  [GPU] GB300 hierarchical min      (--variant cl|vl|auto)
 //   122  [GPU] GB300 hierarchical argmin
 // The reference's own ids 16 (CL) and 20 (VL) name its kernels; their GB300
-// counterparts are 22 --variant cl and 22 --variant vl.
+// counterparts are 22 --variant cl and 22 --variant vl; its CL ablations 23, 24
+// and 19 are 22 --variant cl-noshuffle, cl-tile and cl-atomic.
 #include <getopt.h>
 #include <omp.h>
 #include <unistd.h>
@@ -117,13 +118,27 @@ void print_help() {
                  "  --data-dir <dir>        where those files go (default .)\n"
                  "  --log_build_threshold[=<k>]  accepted for command-line compatibility (no effect here)\n"
                  "  --save-power[=<file>]   accepted for command-line compatibility (power is not measured)\n"
-                 "  --variant cl|vl|auto    work distribution of alg 22/122 (default auto)\n"
+                 "  --variant <name>        work distribution of alg 22/122: auto (default), vl, cl, and the\n"
+                 "                          reference's ablations of cl: cl-noshuffle (its alg 23), cl-tile\n"
+                 "                          (alg 24), cl-atomic (alg 19)\n"
                  "  --rf_log <3..5>         log2 of the per-level reduction factor (default: the variant's)\n"
                  "  --lanes <2|4|8|16|32>   CL lanes per query\n"
                  "  --l2_persist            put the coarse levels in an L2 persisting window\n"
                  "  --ties <frac>           set that fraction of the entries to the array's minimum\n"
                  "  --hbm_peak <GB/s>       peak for the CSV roofline_frac column (default: the device's\n"
                  "                          theoretical rate from its memory clock and bus width)\n");
+}
+
+// --variant names: the GB300 work distributions, and the reference's
+// ablations of CL (its algs 23, 24 and 19) as work distributions of alg 22.
+int variant_code(const std::string& v) {
+    if (v == "cl") return RMQ_VARIANT_CL;
+    if (v == "vl") return RMQ_VARIANT_VL;
+    if (v == "cl-noshuffle") return RMQ_VARIANT_CL_NO_SHUFFLE;
+    if (v == "cl-tile") return RMQ_VARIANT_CL_QUERY_PER_TILE;
+    if (v == "cl-atomic") return RMQ_VARIANT_CL_ATOMIC;
+    if (v == "auto") return RMQ_VARIANT_AUTO;
+    return -1;
 }
 
 bool parse(int argc, char** argv, Args& a) {
@@ -229,6 +244,10 @@ bool parse(int argc, char** argv, Args& a) {
             case O_PEAK: a.hbm_peak = std::atof(optarg); break;
             default: print_help(); return false;
         }
+    }
+    if (variant_code(a.variant) < 0) {
+        std::fprintf(stderr, "Error: unknown --variant %s\n", a.variant.c_str());
+        return false;
     }
     // the default t = 2^15 is also clamped to log2(n)
     while (a.log_bs > 0 && (uint64_t(1) << a.log_bs) > a.n) --a.log_bs;
@@ -377,7 +396,7 @@ Result run_alg(const Args& a, const float* hA, const uint32_t* hQ, const float* 
     if (a.alg == ALG_GB300 || a.alg == ALG_GB300_IDX) {
         rmq_config cfg;
         rmq_config_init(&cfg);
-        cfg.variant = a.variant == "cl" ? RMQ_VARIANT_CL : a.variant == "vl" ? RMQ_VARIANT_VL : RMQ_VARIANT_AUTO;
+        cfg.variant = variant_code(a.variant);
         cfg.scan_threshold = uint64_t(1) << a.log_bs;
         cfg.rf_log = a.rf_log;
         cfg.lanes = a.lanes;
@@ -617,7 +636,8 @@ int main(int argc, char** argv) {
     if (a.alg == 16 || a.alg == 20 || a.alg == 17 || a.alg == 18 || a.alg == 19 || a.alg == 21 ||
         a.alg == 23 || a.alg == 24) {
         std::fprintf(stderr, "Error: alg %d is one of the reference's own kernels; this driver runs "
-                             "alg 22 --variant cl (CL) or --variant vl (VL)\n", a.alg);
+                             "alg 22 --variant cl (CL, alg 16), vl (VL, alg 20), cl-noshuffle (alg 23), "
+                             "cl-tile (alg 24) or cl-atomic (alg 19)\n", a.alg);
         return EXIT_FAILURE;
     }
     if (std::string(alg_name(a.alg)).empty()) {

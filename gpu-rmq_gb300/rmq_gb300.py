@@ -39,7 +39,11 @@ RMQ_ERR_UNSUPPORTED = 7
 VARIANT_AUTO = 0
 VARIANT_CL = 1
 VARIANT_VL = 2
-VARIANTS = {"auto": VARIANT_AUTO, "cl": VARIANT_CL, "vl": VARIANT_VL}
+VARIANT_CL_NO_SHUFFLE = 3      # the reference's ablations of CL (algs 23, 24, 19)
+VARIANT_CL_QUERY_PER_TILE = 4
+VARIANT_CL_ATOMIC = 5
+VARIANTS = {"auto": VARIANT_AUTO, "cl": VARIANT_CL, "vl": VARIANT_VL, "cl-noshuffle": VARIANT_CL_NO_SHUFFLE,
+            "cl-tile": VARIANT_CL_QUERY_PER_TILE, "cl-atomic": VARIANT_CL_ATOMIC}
 
 NO_POS = 0xFFFFFFFF
 

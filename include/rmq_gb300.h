@@ -49,7 +49,13 @@ typedef enum {
 typedef enum {
     RMQ_VARIANT_AUTO = 0,  /* the measured best: VL with rf = 8                                          */
     RMQ_VARIANT_CL = 1,    /* tile of lanes answering its queries one after another (reference alg 16 family) */
-    RMQ_VARIANT_VL = 2     /* one thread per query, 256-bit loads (reference alg 20 family)              */
+    RMQ_VARIANT_VL = 2,    /* one thread per query, 256-bit loads (reference alg 20 family)              */
+    /* The reference's ablations of its CL kernel: the same hierarchy and
+     * results, other work distributions (src/xxx.h:302-790). */
+    RMQ_VARIANT_CL_NO_SHUFFLE = 3,     /* each lane loads the turn's query itself (alg 23)              */
+    RMQ_VARIANT_CL_QUERY_PER_TILE = 4, /* one query per tile of lanes, no turns (alg 24)               */
+    RMQ_VARIANT_CL_ATOMIC = 5          /* lanes combine with atomic minima, no shuffle reduction (alg 19);
+                                          scan threshold below 2^27                                      */
 } rmq_variant;
 
 typedef struct {

@@ -37,6 +37,8 @@ def test_help_and_bad_arguments():
     r = run(100, 10, -1, 16)
     assert r.returncode != 0 and "variant cl" in r.stderr  # reference-only kernel ids
     assert run(100, 10, -1, 5).returncode != 0  # not in this driver
+    r = run(100, 10, -1, 22, "--variant", "cl-fast")
+    assert r.returncode != 0 and "unknown --variant" in r.stderr
 
 
 @pytest.mark.parametrize("alg", [0, 100])
@@ -62,6 +64,8 @@ def test_cpu_algorithms_and_csv(tmp_path, alg):
 @pytest.mark.parametrize("alg,extra", [
     (22, ["--variant", "vl"]), (22, ["--variant", "cl"]), (122, ["--variant", "auto"]),
     (122, ["--variant", "cl", "--rf_log", "5", "--lanes", "16"]), (2, []), (102, []),
+    (22, ["--variant", "cl-noshuffle", "--rf_log", "5", "--lanes", "16"]), (122, ["--variant", "cl-tile"]),
+    (122, ["--variant", "cl-atomic", "--lanes", "8"]),
 ])
 @pytest.mark.parametrize("check", ["--check", "--randTrivialCheck", "--trivialCheck"])
 def test_gpu_algorithms_pass_checks(cuda, tmp_path, alg, extra, check):

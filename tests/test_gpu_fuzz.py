@@ -14,7 +14,7 @@ from oracle import oracle
 pytestmark = pytest.mark.gpu
 
 CFGS = [("vl", 3, 0), ("vl", 4, 0), ("vl", 5, 0), ("cl", 3, 2), ("cl", 4, 4), ("cl", 5, 8), ("cl", 3, 32),
-        ("cl", 5, 16)]
+        ("cl", 5, 16), ("cl-noshuffle", 4, 8), ("cl-tile", 3, 4), ("cl-atomic", 5, 16)]
 BOUNDARY_SIZES = [1, 2, 7, 8, 9, 15, 16, 17, 63, 64, 65, 511, 512, 513, 4095, 4096, 4097, 8191, 8192, 8193,
                   16383, 16384, 16385, 32768, 131071, 131072, 131073, 1 << 20]
 
@@ -34,7 +34,7 @@ def _case(rng):
         a = rng.random(n).astype(np.float32)
         a[rng.integers(0, n, max(1, n // 50))] = a.min()
     v, rf_log, lanes = CFGS[int(rng.integers(0, len(CFGS)))]
-    tmin = (2 if v == "cl" else 1) << rf_log
+    tmin = (2 if v.startswith("cl") else 1) << rf_log
     t = int(rng.choice([0, tmin, tmin + 1, 32, 64, 100, 1024, 1 << 14, 1 << 16, n + 5]))
     t = max(t, tmin) if t else 0
     q = int(rng.integers(1, 8000))

@@ -21,14 +21,17 @@ pytestmark = pytest.mark.gpu
 # (variant, rf_log, lanes) configurations exercised everywhere
 CONFIGS = [("vl", 3, 0), ("vl", 4, 0), ("vl", 5, 0),
            ("cl", 5, 8), ("cl", 5, 4), ("cl", 5, 16), ("cl", 5, 32),
-           ("cl", 3, 8), ("cl", 4, 16), ("cl", 3, 32), ("cl", 3, 2), ("cl", 4, 2)]
+           ("cl", 3, 8), ("cl", 4, 16), ("cl", 3, 32), ("cl", 3, 2), ("cl", 4, 2),
+           # the reference's ablations of CL (algs 23, 24, 19) as work distributions
+           ("cl-noshuffle", 5, 16), ("cl-noshuffle", 3, 2), ("cl-tile", 5, 16), ("cl-tile", 3, 8),
+           ("cl-atomic", 5, 16), ("cl-atomic", 3, 2), ("cl-atomic", 4, 32)]
 CFG_IDS = [f"{v}-rf{1 << r}-g{g}" for v, r, g in CONFIGS]
 
 
 def _t_for(variant, rf_log, t=None):
     rf = 1 << rf_log
     if t is not None:
-        return max(t, 2 * rf if variant == "cl" else rf)
+        return max(t, 2 * rf if variant.startswith("cl") else rf)
     return 0
 
 
@@ -309,3 +312,20 @@ def test_streamed_build_sizes(cuda, n):
     torch.cuda.synchronize()
     assert torch.equal(m64.view(torch.int32), bm.view(torch.int32)), "64-bit min"
     assert torch.equal(i64, bi.to(torch.int64)), "64-bit argmin"
+
+
+def test_cl_ablations_preconditions_and_info(cuda):
+    """The ablated CL work distributions keep CL's precondition t >= 2 rf and
+    report their variant; the atomic combine takes thresholds below 2^27."""
+    import torch
+    a = torch.zeros(1 << 12, dtype=torch.float32, device=cuda)
+    for v, code in (("cl-noshuffle", 3), ("cl-tile", 4), ("cl-atomic", 5)):
+        with pytest.raises(R.RMQError) as e:
+            R.Hierarchy(a, variant=v, t=31, rf_log=4)  # t < 2 rf
+        assert e.value.status == R.RMQ_ERR_ARG
+        with R.Hierarchy(a, variant=v, t=64, rf_log=4, lanes=4) as h:
+            info = h.info()
+            assert info.variant == code and info.lanes == 4 and info.rf_log == 4
+    with pytest.raises(R.RMQError) as e:
+        R.Hierarchy(a, variant="cl-atomic", t=1 << 27, rf_log=3)
+    assert e.value.status == R.RMQ_ERR_UNSUPPORTED
