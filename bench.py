@@ -1051,7 +1051,7 @@ def run_batched(args, ws, rank, local):
         print(json.dumps(line), flush=True)
 
 
-def serve_trace(rng, sizes, seconds, rate, reg_frac, seed):
+def serve_trace(rng, sizes, seconds, rate, reg_frac, seed, max_log2: float = 26.0):
     """Poisson request stream: arrivals at `rate`/s for `seconds`; a fraction
     reg_frac registers a new array (size law of the resident ones), the rest
     are requests naming a registered array, with 1..2^16 queries (log-uniform)
@@ -1070,7 +1070,7 @@ def serve_trace(rng, sizes, seconds, rate, reg_frac, seed):
     req_n = np.zeros(E, dtype=np.int64)
     for i in range(E):
         if is_reg[i]:
-            n = int(np.exp(rng.uniform(np.log(2.0 ** 16), np.log(2.0 ** 26))))
+            n = int(np.exp(rng.uniform(np.log(2.0 ** 16), np.log(2.0 ** max_log2))))
             ev["kind"][i] = 1
             ev["n"][i] = n
             ev["seed"][i] = seed * 1000003 + len(n_of)
@@ -1117,9 +1117,10 @@ def served_record(args, ws, rank, dev) -> dict:
         tp = now
 
     rng = np.random.default_rng(args.seed + rank)
-    sizes = [int(np.exp(rng.uniform(np.log(2.0 ** 16), np.log(2.0 ** 26)))) for _ in range(256)]
+    top = float(args.serve_max_log2)
+    sizes = [int(np.exp(rng.uniform(np.log(2.0 ** 16), np.log(2.0 ** top)))) for _ in range(args.serve_arrays)]
     seed_of = lambda a: args.seed * 1000003 + a  # noqa: E731  (the trace uses the same rule)
-    ev, lr_pageable, n_of = serve_trace(rng, sizes, args.serve_seconds, 20000.0, 0.05, args.seed)
+    ev, lr_pageable, n_of = serve_trace(rng, sizes, args.serve_seconds, 20000.0, 0.05, args.seed, top)
     req = ev["kind"] == 0
     Q = int(ev["q"][req].sum())
     mark("trace")
@@ -1148,7 +1149,8 @@ def served_record(args, ws, rank, dev) -> dict:
         wsrv.replay(wev, wlr, np.empty(wq, np.uint32), np.empty(wq, np.float32))
     mark("warmup_server")
 
-    srv = R.Server(hbm_budget_bytes=64 << 30, slots=args.serve_slots, t=64, query_threads=args.serve_threads)
+    srv = R.Server(hbm_budget_bytes=int(args.serve_budget_gib * (1 << 30)), slots=args.serve_slots, t=64,
+                   query_threads=args.serve_threads)
     for a, n in enumerate(sizes):
         srv.register_generated(n, seed_of(a))
     warm = np.zeros((1, 2), dtype=np.uint32)
@@ -1212,9 +1214,9 @@ def served_record(args, ws, rank, dev) -> dict:
     return {
         "metric": "RMQ queries/s (served: continuous batching)", "value": Q / wall, "unit": UNIT,
         "steps": 1, "warmup": 1, "ms_per_step": wall * 1e3,
-        "workload": "serving: 256 resident arrays log-uniform [2^16, 2^26], Poisson 20k req/s, "
-                    "1..2^16 queries per request (log-uniform), lognormal(2^13, 1) lengths, "
-                    "5 % registrations, 64 GiB budget, LRU eviction",
+        "workload": f"serving: {args.serve_arrays} resident arrays log-uniform [2^16, 2^{args.serve_max_log2:g}], "
+                    "Poisson 20k req/s, 1..2^16 queries per request (log-uniform), lognormal(2^13, 1) lengths, "
+                    f"5 % registrations, {args.serve_budget_gib:g} GiB budget, LRU eviction",
         "data": "synthetic (seeded Poisson trace)",
         "seconds": args.serve_seconds, "events": int(ev.size), "requests": int(req.sum()),
         "queries": Q, "slots": args.serve_slots, "seed": args.seed,
@@ -1266,6 +1268,12 @@ def parse_args(argv=None):
                          + ", ".join(SUB_RECORDS))
     ap.add_argument("--serve-seconds", dest="serve_seconds", type=float, default=2.0)
     ap.add_argument("--serve-slots", dest="serve_slots", type=int, default=4)
+    ap.add_argument("--serve-arrays", dest="serve_arrays", type=int, default=256,
+                    help="initially resident arrays of the served workload (a smaller case for profiling)")
+    ap.add_argument("--serve-max-log2", dest="serve_max_log2", type=float, default=26.0,
+                    help="largest served array size, as log2 (sizes are log-uniform from 2^16)")
+    ap.add_argument("--serve-budget-gib", dest="serve_budget_gib", type=float, default=64.0,
+                    help="HBM budget of the server, GiB")
     ap.add_argument("--serve-threads", dest="serve_threads", type=int, default=0,
                     help="CTA size of the served query kernel (0 = library default)")
     ap.add_argument("--batch-arrays", dest="batch_arrays", type=int, default=4096)
