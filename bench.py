@@ -889,10 +889,39 @@ def host_link_rates(h_q, h_idx, h_min, d_idx, d_min, reps: int = 3) -> dict:
         torch.cuda.synchronize()
         return nbytes / (e0.elapsed_time(e1) / reps / 1e3) / 1e9
 
+    # The same copies split into four chunks on four streams each way (more
+    # copy engines at work): whether one engine per direction limits the rate.
+    k = 4
+    ups, downs = [torch.cuda.Stream() for _ in range(k)], [torch.cuda.Stream() for _ in range(k)]
+    cq, cr = h_q.numel() // k, h_idx.numel() // k
+
+    def split(direction_up: bool, direction_down: bool):
+        def fn():
+            for i in range(k):
+                lo_q, hi_q = i * cq, (h_q.numel() if i == k - 1 else (i + 1) * cq)
+                lo_r, hi_r = i * cr, (h_idx.numel() if i == k - 1 else (i + 1) * cr)
+                if direction_up:
+                    ups[i].wait_stream(cur)
+                    with torch.cuda.stream(ups[i]):
+                        d_q[lo_q:hi_q].copy_(h_q[lo_q:hi_q], non_blocking=True)
+                if direction_down:
+                    downs[i].wait_stream(cur)
+                    with torch.cuda.stream(downs[i]):
+                        h_idx[lo_r:hi_r].copy_(d_idx[lo_r:hi_r], non_blocking=True)
+                        h_min[lo_r:hi_r].copy_(d_min[lo_r:hi_r], non_blocking=True)
+            for i in range(k):
+                cur.wait_stream(ups[i])
+                cur.wait_stream(downs[i])
+        return fn
+
     nq = h_q.numel() * 4
     nr = h_idx.numel() * 4 + h_min.numel() * 4
     out = {"h2d_GBps": rate(up, nq), "d2h_GBps": rate(down, nr), "duplex_GBps": rate(both, nq + nr),
-           "what": "copy-engine rates of the same buffers (page-locked host <-> device)"}
+           "h2d_GBps_4_streams": rate(split(True, False), nq),
+           "d2h_GBps_4_streams": rate(split(False, True), nr),
+           "duplex_GBps_4_streams": rate(split(True, True), nq + nr),
+           "what": "copy-engine rates of the same buffers (page-locked host <-> device), "
+                   "one stream per direction and four chunks on four streams per direction"}
     del d_q
     return out
 
