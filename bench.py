@@ -592,6 +592,8 @@ def run_ours(args, ws, rank, local):
 
     # --- end to end: pinned host queries -> device -> host results -------------
     e2e = run_e2e(args, h, qs, dev, ws, ctx["out_idx"], ctx["out_min"], ctx["dq"])
+    ref_style = reference_style_timing(h, ctx, args, stream)
+    sweep = t_sweep(ctx, args, dev, stream) if args.t_sweep else None
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -640,7 +642,10 @@ def run_ours(args, ws, rank, local):
         "min_only_queries_per_s": rec["min_only_queries_per_s"],
         "reference_gpu": reference_gpu,
         "hierarchy": rec["hierarchy"],
+        "reference_style_timing": ref_style,
     }
+    if sweep is not None:
+        line["t_sweep"] = sweep
     h.close()
     del ctx
     gc.collect()
@@ -674,6 +679,75 @@ def run_ours(args, ws, rank, local):
     if ws > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def reference_style_timing(h, ctx, args, stream) -> dict:
+    """The reference's own way of timing a query run (src/xxx.h:276-283): the
+    host clock around each launch followed by a device synchronisation, one
+    launch per repetition.  Reported beside the CUDA-event figure."""
+    import torch
+    q = ctx["qs"].shape[0]
+    lr_ptr, idx_ptr, min_ptr = int(ctx["dq"].data_ptr()), int(ctx["out_idx"].data_ptr()), int(ctx["out_min"].data_ptr())
+    sh = stream.cuda_stream
+    times = []
+    for k in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        st = h.query_idx_raw(lr_ptr, q, idx_ptr, min_ptr, sh)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        if st != 0:
+            raise RuntimeError(f"rmq_query_idx failed: {st}")
+        if k >= args.warmup:
+            times.append(dt * 1e3)
+    med = statistics.median(times)
+    return {"ms_median": med, "ms_mean": statistics.mean(times), "queries_per_s_median": q / (med / 1e3),
+            "reps": len(times),
+            "what": "host clock around one launch + device synchronisation per repetition, the reference's "
+                    "timed loop (src/xxx.h:276-283); `value` uses CUDA events"}
+
+
+T_SWEEP = (32, 64, 1 << 10, 1 << 12, 1 << 14, 1 << 16)
+
+
+def t_sweep(ctx, args, dev, stream) -> dict:
+    """The headline workload's queries over hierarchies built with other scan
+    thresholds (the reference's `t`; the paper uses 64 for CL, 32 for VL):
+    queries/s by CUDA events per launch and whether the results equal the
+    headline's bit for bit."""
+    import torch
+    import rmq_gb300 as R
+    q = ctx["qs"].shape[0]
+    dq = ctx["dq"]
+    ref_min, ref_idx = ctx["out_min"], ctx["out_idx"]
+    out_min = torch.empty_like(ref_min)
+    out_idx = torch.empty_like(ref_idx)
+    sh = stream.cuda_stream
+    steps = max(1, min(args.steps, 5))
+    out = {}
+    for t in T_SWEEP:
+        h = R.Hierarchy(ctx["dv"], variant=args.variant, t=t, rf_log=args.rf_log, lanes=args.lanes, stream=stream)
+        info = h.info()
+        args_ptrs = (int(dq.data_ptr()), q, int(out_idx.data_ptr()), int(out_min.data_ptr()), sh)
+        with torch.cuda.stream(stream):
+            for _ in range(2):
+                if h.query_idx_raw(*args_ptrs) != 0:
+                    raise RuntimeError("rmq_query_idx failed")
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        with torch.cuda.stream(stream):
+            ev[0].record(stream)
+            for _ in range(steps):
+                h.query_idx_raw(*args_ptrs)
+            ev[1].record(stream)
+        torch.cuda.synchronize()
+        ms = ev[0].elapsed_time(ev[1]) / steps
+        same = bool(torch.equal(out_idx, ref_idx) and torch.equal(out_min.view(torch.int32), ref_min.view(torch.int32)))
+        out[str(t)] = {"queries_per_s": q / (ms / 1e3), "ms": ms, "levels": int(info.num_levels),
+                       "results_equal_headline": same}
+        h.close()
+    del out_min, out_idx
+    return {"by_t": out, "steps": steps, "variant": args.variant,
+            "what": "the headline's queries and array, hierarchy rebuilt per scan threshold t"}
 
 
 def targets_summary(subs: dict) -> dict:
@@ -1317,6 +1391,8 @@ def parse_args(argv=None):
     ap.add_argument("--rf-log", dest="rf_log", type=int, default=0)
     ap.add_argument("--lanes", type=int, default=0)
     ap.add_argument("--l2-persist", dest="l2_persist", action="store_true")
+    ap.add_argument("--no-t-sweep", dest="t_sweep", action="store_false",
+                    help="skip the scan-threshold sweep of the headline workload")
     ap.add_argument("--cpu-budget", dest="cpu_budget", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", dest="no_cpu_baseline", action="store_true")
     ap.add_argument("--no-reference-gpu", dest="no_reference_gpu", action="store_true")
