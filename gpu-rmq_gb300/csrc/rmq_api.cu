@@ -340,6 +340,10 @@ static int query_common(const rmq_handle* hc, const void* d_lr, uint64_t q, floa
     const uintptr_t qalign = wide_call ? 15u : 7u;
     if (d_lr == nullptr || (reinterpret_cast<uintptr_t>(d_lr) & qalign) != 0) return RMQ_ERR_ARG;
     if (d_min == nullptr && d_argmin == nullptr) return RMQ_ERR_ARG;
+    // results are stored element by element: each pointer must be aligned to its element
+    if ((reinterpret_cast<uintptr_t>(d_min) & 3u) != 0 ||
+        (reinterpret_cast<uintptr_t>(d_argmin) & (wide_call ? 7u : 3u)) != 0)
+        return RMQ_ERR_ARG;
     if (d_argmin != nullptr && !hc->with_index && hc->lay.num_levels > 1) return RMQ_ERR_NO_INDEX;
     rmq_handle* h = const_cast<rmq_handle*>(hc);
     DeviceGuard guard(h->device);
@@ -422,18 +426,22 @@ static cudaError_t ensure_pipe(rmq_handle* h, uint64_t chunk) {
     return cudaSuccess;
 }
 
-// Device address of host memory the device can read and write directly
-// (page-locked: cudaHostAlloc / cudaHostRegister), aligned to `align` bytes;
-// nullptr otherwise.
-static void* mapped_host(const void* p, uintptr_t align) {
-    if (p == nullptr || (reinterpret_cast<uintptr_t>(p) & (align - 1)) != 0) return nullptr;
-    cudaPointerAttributes at;
-    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+// Device address of host memory [p, p + bytes) that the device can read and
+// write directly (page-locked: cudaHostAlloc / cudaHostRegister), aligned to
+// `align` bytes; nullptr when any of it is not (the first and the last byte
+// must map into one contiguous device range), so such buffers are staged.
+static void* mapped_host(const void* p, size_t bytes, uintptr_t align) {
+    if (p == nullptr || bytes == 0 || (reinterpret_cast<uintptr_t>(p) & (align - 1)) != 0) return nullptr;
+    cudaPointerAttributes a0, a1;
+    const char* last = static_cast<const char*>(p) + (bytes - 1);
+    if (cudaPointerGetAttributes(&a0, p) != cudaSuccess || cudaPointerGetAttributes(&a1, last) != cudaSuccess) {
         cudaGetLastError();
         return nullptr;
     }
-    if (at.type != cudaMemoryTypeHost || at.devicePointer == nullptr) return nullptr;
-    return at.devicePointer;
+    if (a0.type != cudaMemoryTypeHost || a1.type != cudaMemoryTypeHost || a0.devicePointer == nullptr ||
+        a1.devicePointer != static_cast<char*>(a0.devicePointer) + (bytes - 1))
+        return nullptr;
+    return a0.devicePointer;
 }
 
 // Host-buffer queries.  When every host buffer is page-locked, one kernel
@@ -459,9 +467,9 @@ static int query_host_common(const rmq_handle* hc, const void* h_lr, uint64_t q,
     const size_t qsize = wide_call ? 2 * sizeof(uint64_t) : 2 * sizeof(uint32_t);
     const size_t isize = wide_call ? sizeof(uint64_t) : sizeof(uint32_t);
 
-    void* m_lr = mapped_host(h_lr, qsize);
-    void* m_min = h_min != nullptr ? mapped_host(h_min, sizeof(float)) : nullptr;
-    void* m_idx = h_argmin != nullptr ? mapped_host(h_argmin, isize) : nullptr;
+    void* m_lr = mapped_host(h_lr, q * qsize, qsize);
+    void* m_min = h_min != nullptr ? mapped_host(h_min, q * sizeof(float), sizeof(float)) : nullptr;
+    void* m_idx = h_argmin != nullptr ? mapped_host(h_argmin, q * isize, isize) : nullptr;
     if (m_lr != nullptr && (h_min == nullptr || m_min != nullptr) && (h_argmin == nullptr || m_idx != nullptr)) {
         cudaError_t e = ensure_pipe(h, 0);
         if (e != cudaSuccess) return cuda_status(e);
@@ -589,7 +597,10 @@ int rmq_scan_bruteforce(const float* d_values, uint64_t n, const uint32_t* d_lr,
     if (d_values == nullptr || n == 0 || d_lr == nullptr) return RMQ_ERR_ARG;
     if (d_min_or_null == nullptr && d_argmin_or_null == nullptr) return RMQ_ERR_ARG;
     if (n > kMaxN || q > 0xFFFFFFFFull) return RMQ_ERR_UNSUPPORTED;
-    if ((reinterpret_cast<uintptr_t>(d_lr) & 7u) != 0) return RMQ_ERR_ARG;
+    if ((reinterpret_cast<uintptr_t>(d_lr) & 7u) != 0 || (reinterpret_cast<uintptr_t>(d_values) & 3u) != 0 ||
+        (reinterpret_cast<uintptr_t>(d_min_or_null) & 3u) != 0 ||
+        (reinterpret_cast<uintptr_t>(d_argmin_or_null) & 3u) != 0)
+        return RMQ_ERR_ARG;
     return cuda_status(rmq::launch_bruteforce(d_values, uint32_t(n), reinterpret_cast<const uint2*>(d_lr),
                                               uint32_t(q), d_min_or_null, d_argmin_or_null,
                                               reinterpret_cast<cudaStream_t>(stream)));

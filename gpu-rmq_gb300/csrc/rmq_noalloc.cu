@@ -112,6 +112,8 @@ extern "C" int rmq_query_idx_static(const float* d_values, uint64_t n, uint64_t 
     if (d_values == nullptr || n == 0 || d_argmin == nullptr) return RMQ_ERR_ARG;
     if ((reinterpret_cast<uintptr_t>(d_values) & 31u) != 0) return RMQ_ERR_ARG;
     if (q > 0 && (d_lr == nullptr || (reinterpret_cast<uintptr_t>(d_lr) & 7u) != 0)) return RMQ_ERR_ARG;
+    if ((reinterpret_cast<uintptr_t>(d_argmin) & 3u) != 0 || (reinterpret_cast<uintptr_t>(d_min_or_null) & 3u) != 0)
+        return RMQ_ERR_ARG;
     if (n > kStaticMaxN || q > 0xFFFFFFFFull) return RMQ_ERR_UNSUPPORTED;  // above the fixed scratch
     const uint64_t t = scan_threshold != 0 ? scan_threshold : kStaticDefaultT;
     if (t < (uint64_t(1) << kStaticRfLog)) return RMQ_ERR_ARG;  // VL precondition, src/xxx.h:938

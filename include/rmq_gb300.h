@@ -108,6 +108,9 @@ int rmq_query(const rmq_handle* h, const uint32_t* d_lr, uint64_t q, float* d_mi
  * cpu_rmq_idx (src/cpu_methods.h:56). */
 int rmq_query_idx(const rmq_handle* h, const uint32_t* d_lr, uint64_t q,
                   uint32_t* d_argmin, float* d_min_or_null, rmq_stream_t stream);
+/* For every query call: d_lr is aligned to its pair (8 bytes; 16 for the
+ * 64-bit forms) and each result pointer to its element (4 bytes; 8 for
+ * 64-bit argmin); anything else returns RMQ_ERR_ARG before any launch. */
 
 /* 64-bit counterparts for handles built with index_bits = 64 (the
  * reference's IS_LONG build: uint64_t indices and ulong2 queries,
@@ -126,9 +129,9 @@ int rmq_query_idx64(const rmq_handle* h, const uint64_t* d_lr, uint64_t q, uint6
  * memory; results are written to host memory.  Blocking: returns when every
  * result is in place; calls on one handle are serialised (on streams the
  * handle owns, created on the first call and kept until rmq_destroy).
- * When every buffer is page-locked (cudaHostAlloc / cudaHostRegister) and
- * naturally aligned, one kernel launch reads the queries from and writes the
- * results to host memory directly.  Otherwise chunks of 2^22 queries go
+ * When every buffer is page-locked (cudaHostAlloc / cudaHostRegister) over
+ * its whole length and naturally aligned, one kernel launch reads the
+ * queries from and writes the results to host memory directly.  Otherwise chunks of 2^22 queries go
  * through device staging buffers (three chunks, allocated on first use and
  * kept), the upload of one chunk and the download of the previous one
  * overlapping the kernel of the current one. */

@@ -103,6 +103,17 @@ def test_bad_arguments_rejected_before_device_work():
     assert L.rmq_scan_bruteforce(0x1000, 10, 0x1004, 1, 0x2000, None, None) == R.RMQ_ERR_ARG
     assert L.rmq_get_info(None, None) == R.RMQ_ERR_ARG
     L.rmq_destroy(None)
+    # values, results off their element alignment (checked before any device work)
+    assert L.rmq_scan_bruteforce(0x1002, 10, 0x1000, 1, 0x2000, None, None) == R.RMQ_ERR_ARG
+    assert L.rmq_scan_bruteforce(0x1000, 10, 0x1000, 1, 0x2002, None, None) == R.RMQ_ERR_ARG
+    assert L.rmq_scan_bruteforce(0x1000, 10, 0x1000, 1, None, 0x2001, None) == R.RMQ_ERR_ARG
+    static = L.rmq_query_idx_static
+    static.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_uint64,
+                       ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    static.restype = ctypes.c_int
+    assert static(0x1000, 10, 0, 0x1000, 1, 0x2002, None, None) == R.RMQ_ERR_ARG
+    assert static(0x1000, 10, 0, 0x1000, 1, 0x2000, 0x3001, None) == R.RMQ_ERR_ARG
+    assert static(0x1010, 10, 0, 0x1000, 1, 0x2000, None, None) == R.RMQ_ERR_ARG
 
 
 def test_regular_build_has_no_bounds_counter():

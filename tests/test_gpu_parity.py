@@ -177,6 +177,16 @@ def test_argument_errors(cuda):
         assert e.value.status == R.RMQ_ERR_NO_INDEX
         assert h.query_raw(int(q.data_ptr()) + 4, 1, int(a.data_ptr())) == R.RMQ_ERR_ARG
         assert h.query_raw(int(q.data_ptr()), 0, int(a.data_ptr())) == R.RMQ_OK
+    # result pointers off their element alignment are refused before any launch
+    with R.Hierarchy(a, variant="vl") as h:
+        q = torch.zeros(4, dtype=torch.int32, device=cuda)
+        out = torch.zeros(16, dtype=torch.int32, device=cuda)
+        base = int(out.data_ptr())
+        assert h.query_raw(int(q.data_ptr()), 1, base + 2) == R.RMQ_ERR_ARG
+        assert h.query_idx_raw(int(q.data_ptr()), 1, base + 1, base + 16) == R.RMQ_ERR_ARG
+        assert h.query_idx_raw(int(q.data_ptr()), 1, base, base + 18) == R.RMQ_ERR_ARG
+        assert h.query_idx_raw(int(q.data_ptr()), 1, base, base + 16) == R.RMQ_OK
+        torch.cuda.synchronize()
 
 
 def test_bruteforce_checker_matches_oracle(cuda):
