@@ -487,6 +487,8 @@ int rmq_batch_set_queries(rmq_batch* b, const uint32_t* d_lr, const uint64_t* qu
         if (query_offsets[a + 1] < query_offsets[a]) return RMQ_ERR_ARG;
     const uint64_t total = query_offsets[b->num_arrays];
     if (total > 0 && (d_lr == nullptr || (reinterpret_cast<uintptr_t>(d_lr) & 7u) != 0)) return RMQ_ERR_ARG;
+    if ((reinterpret_cast<uintptr_t>(d_argmin) & 3u) != 0 || (reinterpret_cast<uintptr_t>(d_min) & 3u) != 0)
+        return RMQ_ERR_ARG;  // results are stored element by element
     DeviceGuard guard(b->device);
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     b->q_off.assign(query_offsets, query_offsets + b->num_arrays + 1);

@@ -115,6 +115,15 @@ def test_batch_argument_errors(cuda):
         assert e.value.status == R.RMQ_ERR_NO_INDEX
         with pytest.raises(R.RMQError):
             b.run()  # no queries registered
+    with R.Batch(dv, [0, 8], [8, 8]) as b:
+        dq = torch.zeros(4, dtype=torch.int32, device=cuda)
+        out = torch.empty(4, dtype=torch.int32, device=cuda)
+        qo = np.array([0, 1, 2], dtype=np.uint64)
+        set_q = R._bind_batch().rmq_batch_set_queries
+        # result pointers off their 4-byte alignment are refused
+        assert set_q(b._h, dq.data_ptr(), qo.ctypes.data, out.data_ptr() + 2, None, None) == R.RMQ_ERR_ARG
+        assert set_q(b._h, dq.data_ptr(), qo.ctypes.data, out.data_ptr(), out.data_ptr() + 9,
+                     None) == R.RMQ_ERR_ARG
 
 
 def test_device_generators(cuda):
