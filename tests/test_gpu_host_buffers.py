@@ -147,3 +147,56 @@ def test_page_locked_buffers_direct_path(cuda):
             got = raw.numpy()[2:2 + 4 * q].copy().view(np.float32)
             assert got.tobytes() == dm.tobytes()
             assert np.array_equal(pi.numpy().view(np.uint32), di)
+
+
+def test_host_calls_from_several_threads_on_one_handle(cuda):
+    """Host-buffer calls on one handle from several host threads at once
+    (ctypes releases the GIL): the staging pipeline is shared under the
+    handle's lock, page-locked buffers take the direct path; every thread
+    gets exactly its own queries' results."""
+    import threading
+    import torch
+    n = 1 << 20
+    a = R.gen_array(n, 21)
+    dv = torch.from_numpy(a).to(cuda)
+    sets = [R.gen_queries(150001 + 7 * k, -7 if k % 2 else -1, n, 30 + k) for k in range(4)]
+    with R.Hierarchy(dv, variant="vl") as h:
+        expect = []
+        for qs in sets:
+            i, m = h.query_idx(torch.from_numpy(qs.view(np.int32)).to(cuda), with_min=True)
+            expect.append((i.cpu().numpy().view(np.uint32), m.cpu().numpy()))
+        torch.cuda.synchronize()
+        pinned = []
+        for qs in sets:
+            q = qs.shape[0]
+            pinned.append((torch.from_numpy(qs.view(np.int32).reshape(-1)).pin_memory(),
+                           torch.empty(q, dtype=torch.int32).pin_memory(),
+                           torch.empty(q, dtype=torch.float32).pin_memory()))
+        results, errors = {}, []
+
+        def worker(k, direct):
+            try:
+                for _ in range(3):
+                    if direct:
+                        pq, pi, pm = pinned[k]
+                        st = h.query_idx_host_raw(int(pq.data_ptr()), sets[k].shape[0], int(pi.data_ptr()),
+                                                  int(pm.data_ptr()))
+                        assert st == R.RMQ_OK
+                        got = (pi.numpy().view(np.uint32).copy(), pm.numpy().copy())
+                    else:
+                        got = h.query_idx_host(sets[k], with_min=True)
+                    results[(k, direct)] = got
+            except Exception as exc:  # reported to the main thread
+                errors.append(exc)
+
+        threads = [threading.Thread(target=worker, args=(k, d)) for k in range(4) for d in (False, True)]
+        for t in threads:
+            t.start()
+        for t in threads:
+            t.join()
+    assert not errors, errors
+    for (k, direct), (gi, gm) in results.items():
+        ei, em = expect[k]
+        assert np.array_equal(gi, ei), (k, direct)
+        assert gm.tobytes() == em.tobytes(), (k, direct)
+    assert len(results) == 8
