@@ -212,3 +212,60 @@ def test_page_locked_requests_are_answered_in_place(cuda):
         stats = srv.stats()
     # exactly the requests with page-locked buffers were answered in place
     assert stats["direct_requests"] == sum(1 for x in prepared if x[-1])
+
+
+def test_concurrent_submitters_and_registration(cuda):
+    """Several host threads submit to and wait on one server at once (each
+    waiting on its own requests while the others' are in flight) while
+    another thread registers arrays: every request's results equal the
+    oracle and every request completes."""
+    import threading
+    rng = np.random.default_rng(9)
+    sizes = [5000, 1 << 16, 123457, 1 << 19]
+    arrays = [(rng.integers(0, 50, n) / 7).astype(np.float32) for n in sizes]
+    errors, done = [], []
+    with R.Server(hbm_budget_bytes=1 << 30, slots=4) as srv:
+        ids = [srv.register_host(a) for a in arrays]
+
+        def check(pending):
+            for rid, aid, qs, oi, om in pending:
+                st, _ = srv.wait(rid)
+                assert st == R.RMQ_OK
+                assert np.array_equal(oi, oracle.rmq_argmin(arrays[aid], qs))
+                assert om.tobytes() == oracle.rmq_min(arrays[aid], qs).tobytes()
+                done.append(rid)
+
+        def submitter(k):
+            try:
+                r = np.random.default_rng(100 + k)
+                pending = []
+                for j in range(40):
+                    aid = int(r.integers(0, len(sizes)))
+                    qs = _queries(r, sizes[aid], int(r.integers(1, 3000)))
+                    oi = np.empty(qs.shape[0], np.uint32)
+                    om = np.empty(qs.shape[0], np.float32)
+                    pending.append((srv.submit(ids[aid], qs, oi, om), aid, qs, oi, om))
+                    if j % 5 == 4:
+                        check(pending)
+                        pending = []
+                check(pending)
+            except Exception as exc:  # reported to the main thread
+                errors.append(exc)
+
+        def registrar():
+            try:
+                for s in range(6):
+                    srv.register_generated(1 << 16, 500 + s)
+            except Exception as exc:
+                errors.append(exc)
+
+        threads = [threading.Thread(target=submitter, args=(k,)) for k in range(4)]
+        threads.append(threading.Thread(target=registrar))
+        for t in threads:
+            t.start()
+        for t in threads:
+            t.join()
+        stats = srv.stats()
+    assert not errors, errors
+    assert len(done) == 4 * 40 and len(set(done)) == 4 * 40
+    assert stats["registrations"] == len(sizes) + 6
