@@ -726,7 +726,12 @@ def t_sweep(ctx, args, dev, stream) -> dict:
     steps = max(1, min(args.steps, 5))
     out = {}
     for t in T_SWEEP:
-        h = R.Hierarchy(ctx["dv"], variant=args.variant, t=t, rf_log=args.rf_log, lanes=args.lanes, stream=stream)
+        try:
+            h = R.Hierarchy(ctx["dv"], variant=args.variant, t=t, rf_log=args.rf_log, lanes=args.lanes,
+                            stream=stream)
+        except R.RMQError as exc:  # below the variant's minimum t (CL: 2 rf, VL: rf)
+            out[str(t)] = {"unsupported": R.strerror(exc.status)}
+            continue
         info = h.info()
         args_ptrs = (int(dq.data_ptr()), q, int(out_idx.data_ptr()), int(out_min.data_ptr()), sh)
         with torch.cuda.stream(stream):
