@@ -500,8 +500,10 @@ def plain_measure(n, q, lr, ties, t, seed, args, dev, stream, ws, *, tag_suffix=
     kernel_ms = statistics.mean(per_launch)
     alg_bytes = algorithmic_bytes_chunked(qs, n)
     achieved = alg_bytes / (kernel_ms / 1e3) / 1e9
-    vname = {1: "cl", 2: "vl", 3: "cl-noshuffle", 4: "cl-tile", 5: "cl-atomic"}.get(int(info.variant), "cl")
-    tag = f"vl-rf{1 << info.rf_log}" if info.variant == 2 else f"{vname}-rf{1 << info.rf_log}-g{info.lanes}"
+    vname = {1: "cl", 2: "vl", 3: "cl-noshuffle", 4: "cl-tile", 5: "cl-atomic",
+             6: "vl-short"}.get(int(info.variant), "cl")
+    is_vl = info.variant in (2, 6)
+    tag = f"{vname}-rf{1 << info.rf_log}" if is_vl else f"{vname}-rf{1 << info.rf_log}-g{info.lanes}"
     tpq = traffic_per_query(tag + tag_suffix)
     l2p = l2_peak(dev)
     l2_sample = qs[: 1 << 20]
@@ -512,9 +514,11 @@ def plain_measure(n, q, lr, ties, t, seed, args, dev, stream, ws, *, tag_suffix=
           "peak_source": "measured here (" + l2p["how"] + ")",
           "sample": f"first {l2_sample.shape[0]} queries",
           "model": "32 B x sectors of levels >= 1 read by the canonical descent (rf 32, t 64)"}
-    kernel = f"query_{'vl' if info.variant == 2 else 'cl'}_kernel (argmin+min), {tag}"
-    if info.variant >= 3:
+    kernel = f"query_{'vl' if is_vl else 'cl'}_kernel (argmin+min), {tag}"
+    if 3 <= info.variant <= 5:
         kernel += " (the reference's ablation of CL as a work distribution)"
+    if info.variant == 6:
+        kernel += " (short-query form: level-0 winners taken in phase 1)"
     if l2_bound:
         # every input of this workload fits in L2: the same algorithmic bytes
         # go against the L2 read rate (inputs are flushed from L2 between steps)
@@ -1391,7 +1395,8 @@ def parse_args(argv=None):
     ap.add_argument("--seed", type=int, default=42)
     ap.add_argument("--ties", type=float, default=0.0,
                     help="fraction of entries set to the global minimum (the large mixed workload uses 0.01)")
-    ap.add_argument("--variant", default="auto", choices=["auto", "cl", "vl", "cl-noshuffle", "cl-tile", "cl-atomic"])
+    ap.add_argument("--variant", default="auto",
+                    choices=["auto", "cl", "vl", "vl-short", "cl-noshuffle", "cl-tile", "cl-atomic"])
     ap.add_argument("--t", type=int, default=1 << 10, help="scan threshold")
     ap.add_argument("--rf-log", dest="rf_log", type=int, default=0)
     ap.add_argument("--lanes", type=int, default=0)

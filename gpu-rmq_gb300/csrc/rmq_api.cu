@@ -102,14 +102,16 @@ int resolve_config(uint64_t n, const rmq_config* cfg_in, int* variant, int* rf_l
     // CL and its three ablated work distributions share the CL preconditions.
     const bool cl = v == RMQ_VARIANT_CL || v == RMQ_VARIANT_CL_NO_SHUFFLE || v == RMQ_VARIANT_CL_QUERY_PER_TILE ||
                     v == RMQ_VARIANT_CL_ATOMIC;
-    if (!cl && v != RMQ_VARIANT_VL) return RMQ_ERR_ARG;
+    // VL and its short-query form share the VL preconditions.
+    const bool vl = v == RMQ_VARIANT_VL || v == RMQ_VARIANT_VL_SHORT;
+    if (!cl && !vl) return RMQ_ERR_ARG;
     int r = cfg.rf_log != 0 ? cfg.rf_log : (cl ? kClRfLog : kVlRfLog);
     if (r < 3 || r > 5) return RMQ_ERR_ARG;
     uint64_t tt = cfg.scan_threshold != 0 ? cfg.scan_threshold : (cl ? kClT : kVlT);
     const uint64_t rf = uint64_t(1) << r;
     // The reference's own preconditions (src/xxx.h:211, src/xxx.h:938).
     if (cl && tt < 2 * rf) return RMQ_ERR_ARG;
-    if (v == RMQ_VARIANT_VL && tt < rf) return RMQ_ERR_ARG;
+    if (vl && tt < rf) return RMQ_ERR_ARG;
     // The atomic combine orders a lane's candidates inside a query with 24
     // bits of sector number: pieces of at most 2^27 entries.
     if (v == RMQ_VARIANT_CL_ATOMIC && tt >= (uint64_t(1) << 27)) return RMQ_ERR_UNSUPPORTED;
@@ -211,7 +213,7 @@ int rmq_build(const float* d_values, uint64_t n, const rmq_config* cfg, rmq_stre
     if (bits != 0 && bits != 32 && bits != 64) return RMQ_ERR_ARG;
     const bool wide = bits == 64 || n > kMaxN;
     if (bits == 32 && n > kMaxN) return RMQ_ERR_UNSUPPORTED;
-    if (wide && v != RMQ_VARIANT_VL) return RMQ_ERR_UNSUPPORTED;  // 64-bit positions: VL only
+    if (wide && v != RMQ_VARIANT_VL && v != RMQ_VARIANT_VL_SHORT) return RMQ_ERR_UNSUPPORTED;  // 64-bit: VL only
 
     rmq_handle* h = new (std::nothrow) rmq_handle();
     if (h == nullptr) return RMQ_ERR_OOM;

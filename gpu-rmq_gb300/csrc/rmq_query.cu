@@ -19,14 +19,16 @@
 
 namespace rmq {
 
-template <int R, bool ARGMIN, typename I>
+// CAP: the short-query variant (RMQ_VARIANT_VL_SHORT), which takes a short
+// query's level-0 winner in phase 1 instead of reading it again in phase 2.
+template <int R, bool ARGMIN, typename I, bool CAP = false>
 __global__ void __launch_bounds__(256)
 query_vl_kernel(LevelsT<I> lv, const typename IdxTraits<I>::Pair* __restrict__ qs, uint64_t q,
                 float* __restrict__ out_min, I* __restrict__ out_idx, uint32_t* __restrict__ err) {
     // No early return: every lane takes part in the warp's long final scans.
     using C = typename IdxTraits<I>::Count;
     const C i = C(blockIdx.x) * blockDim.x + threadIdx.x;
-    vl_answer<R, ARGMIN>(lv, qs, i, i < q, out_min, out_idx, err);
+    vl_answer<R, ARGMIN, I, CAP>(lv, qs, i, i < q, out_min, out_idx, err);
 }
 
 // ---------------------------------------------------------------------------
@@ -400,15 +402,21 @@ static cudaError_t launch_query_r(const QueryArgs& a, cudaStream_t s) {
     const bool argmin = a.out_idx != nullptr || a.out_idx64 != nullptr;
     const uint32_t grid = uint32_t((a.q + kQueryBlock - 1u) / kQueryBlock);
     if (a.wide) {
-        // 64-bit positions: the VL kernel only.
-        if (a.variant != 2) return cudaErrorNotSupported;
+        // 64-bit positions: the VL kernel only (the short-query variant is VL here).
+        if (a.variant != 2 && a.variant != 6) return cudaErrorNotSupported;
         const ulonglong2* qs = reinterpret_cast<const ulonglong2*>(a.qs64);
         return argmin ? launch_with_window(query_vl_kernel<R, true, uint64_t>, grid, kQueryBlock, a, s, a.lv64,
                                              qs, a.q, a.out_min, a.out_idx64, a.err)
                       : launch_with_window(query_vl_kernel<R, false, uint64_t>, grid, kQueryBlock, a, s, a.lv64,
                                              qs, a.q, a.out_min, static_cast<uint64_t*>(nullptr), a.err);
     }
-    if (a.variant == 2) {
+    if (a.variant == 6 && R == 3) {
+        return argmin ? launch_with_window(query_vl_kernel<3, true, uint32_t, true>, grid, kQueryBlock, a, s, a.lv,
+                                           a.qs, a.q, a.out_min, a.out_idx, a.err)
+                      : launch_with_window(query_vl_kernel<3, false, uint32_t, true>, grid, kQueryBlock, a, s, a.lv,
+                                           a.qs, a.q, a.out_min, static_cast<uint32_t*>(nullptr), a.err);
+    }
+    if (a.variant == 2 || a.variant == 6) {
         return argmin ? launch_with_window(query_vl_kernel<R, true, uint32_t>, grid, kQueryBlock, a, s, a.lv,
                                              a.qs, a.q, a.out_min, a.out_idx, a.err)
                       : launch_with_window(query_vl_kernel<R, false, uint32_t>, grid, kQueryBlock, a, s, a.lv,

@@ -130,8 +130,39 @@ __device__ __forceinline__ float sector_min(const float (&v)[8], uint32_t jlo, u
     return fmin3(a, b, fminf(w[6], w[7]));
 }
 
+// First entry of v in [jlo, jhi) equal to sm (the minimum over that range).
+__device__ __forceinline__ uint32_t sector_first(const float (&v)[8], uint32_t jlo, uint32_t jhi, float sm) {
+    uint32_t bits = 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) bits |= (v[j] == sm ? 1u : 0u) << j;
+    const uint32_t range = ((1u << jhi) - 1u) & ~((1u << jlo) - 1u);
+    return uint32_t(__ffs(bits & range) - 1);
+}
+
+// The bits of v[j]: the minimum of a range holding both zeros is -0.0 for
+// min.f32, but the answer carries the bits of the first one.
+__device__ __forceinline__ float sector_bits(const float (&v)[8], uint32_t j, float sm) {
+    if (sm != 0.0f) return sm;
+    float x = v[0];
+#pragma unroll
+    for (int jj = 1; jj < 8; ++jj) x = (uint32_t(jj) == j) ? v[jj] : x;
+    return x;
+}
+
 // Sector-granular position of the first minimum.  meta packs the level
-// (bits 0-7), jlo (bits 8-15) and jhi (bits 16-23); kNoPos = none yet.
+// (bits 0-7), jlo (bits 8-15) and jhi (bits 16-23); kNoPos = none yet.  A
+// level-0 candidate also carries its entry: jhi = jlo + 1 with kPosKnown
+// set, and v holds that entry's own bits, so phase 2 needs no load for it
+// (the sector, read once with evict-first, has usually left L2 by then).
+constexpr uint32_t kPosKnown = 1u << 24;
+// 32-bit handles only: the 64-bit kernels have no registers to spare.
+template <typename I>
+constexpr bool kCapture = sizeof(I) == 4;
+// Only queries this short take their level-0 entries in phase 1 (the
+// short-query variant): a longer query's minimum seldom lies in its level-0
+// pieces.
+constexpr uint32_t kCaptureLen = 512;
+
 template <typename I>
 struct Tracker {
     float v;
@@ -210,14 +241,61 @@ __device__ __forceinline__ void scan_bwd(const LevelsT<I>& lv, uint32_t k, I lo,
 // whose size is bounded by t) are scanned by the whole warp instead of one lane.
 constexpr uint32_t kLongScan = 64;
 
+// Level 0 of a short query's descent (rf = 8; the caller checked that the
+// query spans more than two blocks): both boundary sectors in one round trip,
+// and each side's first minimum taken with its entry and bits (kPosKnown),
+// so that a level-0 winner needs no load in phase 2.
+template <bool ARGMIN, typename I>
+__device__ __forceinline__ float vl_level0_capture(const LevelsT<I>& lv, I& l, I& r, const L2Policies& pol,
+                                                   Tracker<I>& tl, Tracker<I>& tr) {
+    const I nl = (l + 7u) & ~I(7);
+    const I pr = r & ~I(7);
+    float a[8], b[8];
+    const bool has_l = nl > l, has_r = r > pr;
+    const uint32_t lo_j = uint32_t(l & 7u), hi_j = uint32_t(r - pr);
+    if (has_l) load_level_sector(lv, 0u, l & ~I(7), pol, a);
+    if (has_r) load_level_sector(lv, 0u, pr, pol, b);
+    float m = f_inf();
+    if (has_l) {
+        const float sm = sector_min(a, lo_j, 8u);
+        m = fminf(m, sm);
+        if (ARGMIN && sm < tl.v) {
+            const uint32_t j = sector_first(a, lo_j, 8u, sm);
+            tl.v = sector_bits(a, j, sm);
+            tl.s = l & ~I(7);
+            tl.meta = (j << 8) | ((j + 1u) << 16) | kPosKnown;
+        }
+    }
+    if (has_r) {
+        const float sm = sector_min(b, 0u, hi_j);
+        m = fminf(m, sm);
+        if (ARGMIN && sm <= tr.v) {
+            const uint32_t j = sector_first(b, 0u, hi_j, sm);
+            tr.v = sector_bits(b, j, sm);
+            tr.s = pr;
+            tr.meta = (j << 8) | ((j + 1u) << 16) | kPosKnown;
+        }
+    }
+    l = nl >> 3;
+    r = pr >> 3;
+    return m;
+}
+
 // Phase 1 up to (not including) the final piece; returns the running minimum
-// and leaves the final piece [l, r) at level k in the arguments.
-template <int R, bool ARGMIN, typename I>
+// and leaves the final piece [l, r) at level k in the arguments.  With CAP
+// (the short-query variant), a short query's level 0 goes through
+// vl_level0_capture, a separate step before the loop.
+template <int R, bool ARGMIN, typename I, bool CAP = false>
 __device__ __forceinline__ float vl_descend(const LevelsT<I>& lv, I& l, I& r, uint32_t& k,
                                             const L2Policies& pol, Tracker<I>& tl, Tracker<I>& tr) {
     constexpr I RF = I(1) << R;
     float m = f_inf();
     k = 0;
+    if (R == 3 && CAP && kCapture<I> && ARGMIN && r - l <= I(kCaptureLen) && 1u < lv.num_levels &&
+        r - l > 2u * RF) {
+        m = vl_level0_capture<ARGMIN>(lv, l, r, pol, tl, tr);
+        k = 1;
+    }
     while (k + 1 < lv.num_levels && r - l > 2u * RF) {
         const I nl = (l + RF - 1) & ~(RF - 1);
         const I pr = r & ~(RF - 1);
@@ -325,14 +403,14 @@ __device__ __forceinline__ void warp_scan_final(const LevelsT<I>& lv, uint32_t k
 
 // Phase 1 for every lane of the warp (all 32 lanes must call it): private
 // descent and short final scans, then the warp's long final scans one by one.
-template <int R, bool ARGMIN, typename I>
+template <int R, bool ARGMIN, typename I, bool CAP = false>
 __device__ __forceinline__ float vl_phase1(const LevelsT<I>& lv, bool active, I l, I r,
                                            const L2Policies& pol, Tracker<I>& tl, Tracker<I>& tr) {
     float m = f_inf();
     uint32_t k = 0;
     bool is_long = false;
     if (active) {
-        m = vl_descend<R, ARGMIN>(lv, l, r, k, pol, tl, tr);
+        m = vl_descend<R, ARGMIN, I, CAP>(lv, l, r, k, pol, tl, tr);
         if (r - l <= kLongScan) scan_fwd<ARGMIN>(lv, k, l, r, pol, m, tl);
         else is_long = true;
     }
@@ -375,7 +453,7 @@ __device__ __forceinline__ float vl_phase1(const LevelsT<I>& lv, bool active, I 
 // a coarse winner of a 32-bit handle the sector's eight stored level-0
 // indices (one 32-byte sector, level offsets are 32-entry aligned) are loaded
 // together with its values, so the index needs no further round trip.
-template <int R, typename I>
+template <int R, typename I, bool CAP = false>
 __device__ __forceinline__ void vl_locate(const LevelsT<I>& lv, I l, const Tracker<I>& tl, const Tracker<I>& tr,
                                           const L2Policies& pol, float& out_v, I& out_i) {
     const bool right = tr.v < tl.v;
@@ -385,6 +463,12 @@ __device__ __forceinline__ void vl_locate(const LevelsT<I>& lv, I l, const Track
         // outside the contract); the scan's answer is the first entry.
         out_i = l;
         out_v = __ldg(lv.val[0] + l);
+        return;
+    }
+    if (CAP && kCapture<I> && (w.meta & kPosKnown)) {
+        // a level-0 winner: its entry and bits were taken in phase 1
+        out_i = w.s + I((w.meta >> 8) & 0xffu);
+        out_v = w.v;
         return;
     }
     const uint32_t k = w.meta & 0xffu;
@@ -435,7 +519,7 @@ __device__ __forceinline__ void vl_locate(const LevelsT<I>& lv, I l, const Track
 // it (long final scans are shared by the warp).  For a valid query
 // (0 <= l <= r < n) returns true with the minimum in v and, for ARGMIN, the
 // argmin in idx; an invalid or absent (active = false) query returns false.
-template <int R, bool ARGMIN, typename I>
+template <int R, bool ARGMIN, typename I, bool CAP = false>
 __device__ __forceinline__ bool vl_compute(const LevelsT<I>& lv, typename IdxTraits<I>::Pair Q, bool active,
                                            float& v, I& idx) {
     const bool valid = active && Q.x <= Q.y && Q.y < lv.size[0];
@@ -446,11 +530,11 @@ __device__ __forceinline__ bool vl_compute(const LevelsT<I>& lv, typename IdxTra
     tracker_init(tr);
     idx = IdxTraits<I>::none;
     if (ARGMIN) {
-        vl_phase1<R, true>(lv, valid, l, r, pol, tl, tr);
+        vl_phase1<R, true, I, CAP>(lv, valid, l, r, pol, tl, tr);
         v = f_nan();
-        if (valid) vl_locate<R>(lv, l, tl, tr, pol, v, idx);
+        if (valid) vl_locate<R, I, CAP>(lv, l, tl, tr, pol, v, idx);
     } else {
-        float m = vl_phase1<R, false>(lv, valid, l, r, pol, tl, tr);
+        float m = vl_phase1<R, false, I, CAP>(lv, valid, l, r, pol, tl, tr);
         // A zero minimum may be -0.0 or +0.0; the reference returns the bits of
         // the first occurrence.  min.f32 returns -0.0 whenever a -0.0 meets a
         // zero (checked on sm_103a, and by the signed-zero parity cases), so a
@@ -459,8 +543,8 @@ __device__ __forceinline__ bool vl_compute(const LevelsT<I>& lv, typename IdxTra
         // participation).
         const bool zero = valid && __float_as_uint(m) == 0x80000000u;
         if (__any_sync(0xffffffffu, zero)) {
-            vl_phase1<R, true>(lv, zero, l, r, pol, tl, tr);
-            if (zero) vl_locate<R>(lv, l, tl, tr, pol, m, idx);
+            vl_phase1<R, true, I, CAP>(lv, zero, l, r, pol, tl, tr);
+            if (zero) vl_locate<R, I, CAP>(lv, l, tl, tr, pol, m, idx);
         }
         v = valid ? m : f_nan();
     }
@@ -480,7 +564,7 @@ __device__ __forceinline__ void vl_store(bool in_range, bool valid, float v, I i
 
 // Query i of qs (when in_range) into out_min[i] / out_idx[i]; every lane of
 // the warp must call it.
-template <int R, bool ARGMIN, typename I>
+template <int R, bool ARGMIN, typename I, bool CAP = false>
 __device__ __forceinline__ void vl_answer(const LevelsT<I>& lv, const typename IdxTraits<I>::Pair* __restrict__ qs,
                                           typename IdxTraits<I>::Count i, bool in_range, float* __restrict__ out_min,
                                           I* __restrict__ out_idx, uint32_t* __restrict__ err) {
@@ -490,7 +574,7 @@ __device__ __forceinline__ void vl_answer(const LevelsT<I>& lv, const typename I
     if (in_range) Q = ld_query(qs + i);
     float v;
     I idx;
-    const bool valid = vl_compute<R, ARGMIN>(lv, Q, in_range, v, idx);
+    const bool valid = vl_compute<R, ARGMIN, I, CAP>(lv, Q, in_range, v, idx);
     vl_store<ARGMIN>(in_range, valid, v, idx, out_min != nullptr ? out_min + i : nullptr,
                      ARGMIN ? out_idx + i : nullptr, err);
 }

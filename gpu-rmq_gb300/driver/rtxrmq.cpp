@@ -118,9 +118,9 @@ void print_help() {
                  "  --data-dir <dir>        where those files go (default .)\n"
                  "  --log_build_threshold[=<k>]  accepted for command-line compatibility (no effect here)\n"
                  "  --save-power[=<file>]   accepted for command-line compatibility (power is not measured)\n"
-                 "  --variant <name>        work distribution of alg 22/122: auto (default), vl, cl, and the\n"
-                 "                          reference's ablations of cl: cl-noshuffle (its alg 23), cl-tile\n"
-                 "                          (alg 24), cl-atomic (alg 19)\n"
+                 "  --variant <name>        work distribution of alg 22/122: auto (default), vl, vl-short (vl\n"
+                 "                          for short queries), cl, and the reference's ablations of cl:\n"
+                 "                          cl-noshuffle (its alg 23), cl-tile (alg 24), cl-atomic (alg 19)\n"
                  "  --rf_log <3..5>         log2 of the per-level reduction factor (default: the variant's)\n"
                  "  --lanes <2|4|8|16|32>   CL lanes per query\n"
                  "  --l2_persist            put the coarse levels in an L2 persisting window\n"
@@ -134,6 +134,7 @@ void print_help() {
 int variant_code(const std::string& v) {
     if (v == "cl") return RMQ_VARIANT_CL;
     if (v == "vl") return RMQ_VARIANT_VL;
+    if (v == "vl-short") return RMQ_VARIANT_VL_SHORT;
     if (v == "cl-noshuffle") return RMQ_VARIANT_CL_NO_SHUFFLE;
     if (v == "cl-tile") return RMQ_VARIANT_CL_QUERY_PER_TILE;
     if (v == "cl-atomic") return RMQ_VARIANT_CL_ATOMIC;
@@ -575,7 +576,7 @@ void write_csv(const Args& a, const Result& r, const uint32_t* hQ, int check_cod
     // bs and nb as the reference writes them: 1 and 0 for its hierarchy rows
     // (src/tools.h:385-392), and for every algorithm whose block size it
     // resets (src/tools.h:221-235), which covers all of this driver's.
-    const bool vl = r.info.variant == RMQ_VARIANT_VL;
+    const bool vl = r.info.variant == RMQ_VARIANT_VL || r.info.variant == RMQ_VARIANT_VL_SHORT;
     int size_log = 0;
     while (size_log < 6 && (1 << size_log) < r.info.lanes) ++size_log;
     // XXX_CG_SIZE_LOG: log2 of the lanes per query, 0 for VL (src/tools.h:403);

@@ -42,8 +42,9 @@ VARIANT_VL = 2
 VARIANT_CL_NO_SHUFFLE = 3      # the reference's ablations of CL (algs 23, 24, 19)
 VARIANT_CL_QUERY_PER_TILE = 4
 VARIANT_CL_ATOMIC = 5
+VARIANT_VL_SHORT = 6           # VL for workloads of short queries
 VARIANTS = {"auto": VARIANT_AUTO, "cl": VARIANT_CL, "vl": VARIANT_VL, "cl-noshuffle": VARIANT_CL_NO_SHUFFLE,
-            "cl-tile": VARIANT_CL_QUERY_PER_TILE, "cl-atomic": VARIANT_CL_ATOMIC}
+            "cl-tile": VARIANT_CL_QUERY_PER_TILE, "cl-atomic": VARIANT_CL_ATOMIC, "vl-short": VARIANT_VL_SHORT}
 
 NO_POS = 0xFFFFFFFF
 

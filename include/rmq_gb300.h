@@ -54,8 +54,13 @@ typedef enum {
      * results, other work distributions (src/xxx.h:302-790). */
     RMQ_VARIANT_CL_NO_SHUFFLE = 3,     /* each lane loads the turn's query itself (alg 23)              */
     RMQ_VARIANT_CL_QUERY_PER_TILE = 4, /* one query per tile of lanes, no turns (alg 24)               */
-    RMQ_VARIANT_CL_ATOMIC = 5          /* lanes combine with atomic minima, no shuffle reduction (alg 19);
+    RMQ_VARIANT_CL_ATOMIC = 5,         /* lanes combine with atomic minima, no shuffle reduction (alg 19);
                                           scan threshold below 2^27                                      */
+    /* VL for workloads of short queries (rf 8, 32-bit positions; otherwise
+     * VL): a query of at most 512 entries takes its level-0 winner while it
+     * folds level 0 instead of reading that sector again to locate it, which
+     * its evict-first L2 line seldom survives.  Same results. */
+    RMQ_VARIANT_VL_SHORT = 6
 } rmq_variant;
 
 typedef struct {

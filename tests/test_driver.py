@@ -65,7 +65,7 @@ def test_cpu_algorithms_and_csv(tmp_path, alg):
     (22, ["--variant", "vl"]), (22, ["--variant", "cl"]), (122, ["--variant", "auto"]),
     (122, ["--variant", "cl", "--rf_log", "5", "--lanes", "16"]), (2, []), (102, []),
     (22, ["--variant", "cl-noshuffle", "--rf_log", "5", "--lanes", "16"]), (122, ["--variant", "cl-tile"]),
-    (122, ["--variant", "cl-atomic", "--lanes", "8"]),
+    (122, ["--variant", "cl-atomic", "--lanes", "8"]), (122, ["--variant", "vl-short"]),
 ])
 @pytest.mark.parametrize("check", ["--check", "--randTrivialCheck", "--trivialCheck"])
 def test_gpu_algorithms_pass_checks(cuda, tmp_path, alg, extra, check):

@@ -13,7 +13,7 @@ from oracle import oracle
 
 pytestmark = pytest.mark.gpu
 
-CFGS = [("vl", 3, 0), ("vl", 4, 0), ("vl", 5, 0), ("cl", 3, 2), ("cl", 4, 4), ("cl", 5, 8), ("cl", 3, 32),
+CFGS = [("vl", 3, 0), ("vl-short", 3, 0), ("vl", 4, 0), ("vl", 5, 0), ("cl", 3, 2), ("cl", 4, 4), ("cl", 5, 8), ("cl", 3, 32),
         ("cl", 5, 16), ("cl-noshuffle", 4, 8), ("cl-tile", 3, 4), ("cl-atomic", 5, 16)]
 BOUNDARY_SIZES = [1, 2, 7, 8, 9, 15, 16, 17, 63, 64, 65, 511, 512, 513, 4095, 4096, 4097, 8191, 8192, 8193,
                   16383, 16384, 16385, 32768, 131071, 131072, 131073, 1 << 20]

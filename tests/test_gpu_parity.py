@@ -19,7 +19,7 @@ from oracle import oracle
 pytestmark = pytest.mark.gpu
 
 # (variant, rf_log, lanes) configurations exercised everywhere
-CONFIGS = [("vl", 3, 0), ("vl", 4, 0), ("vl", 5, 0),
+CONFIGS = [("vl", 3, 0), ("vl-short", 3, 0), ("vl", 4, 0), ("vl", 5, 0),
            ("cl", 5, 8), ("cl", 5, 4), ("cl", 5, 16), ("cl", 5, 32),
            ("cl", 3, 8), ("cl", 4, 16), ("cl", 3, 32), ("cl", 3, 2), ("cl", 4, 2),
            # the reference's ablations of CL (algs 23, 24, 19) as work distributions
