@@ -142,10 +142,11 @@ def build_oracle(force: bool = False) -> Path:
     return ORACLE_LIB
 
 
-def build_reference(force: bool = False) -> Path | None:
-    """Compiles the reference's own CPU path for pinning, when the environment
-    variable RMQ_REFERENCE_ROOT names a reference checkout."""
-    root = os.environ.get("RMQ_REFERENCE_ROOT")
+def build_reference(force: bool = False, reference_root: str | None = None) -> Path | None:
+    """Compiles the reference's own CPU path for pinning, when a reference
+    checkout is named (the argument, else the environment variable
+    RMQ_REFERENCE_ROOT)."""
+    root = reference_root or os.environ.get("RMQ_REFERENCE_ROOT")
     if not root:
         return None
     ref = Path(root)
@@ -157,10 +158,10 @@ def build_reference(force: bool = False) -> Path | None:
     return REF_LIB
 
 
-def build_all(force: bool = False) -> None:
+def build_all(force: bool = False, reference_root: str | None = None) -> None:
     with ThreadPoolExecutor(max_workers=4) as ex:
         futs = [ex.submit(build_library, force), ex.submit(build_generators, force),
-                ex.submit(build_oracle, force), ex.submit(build_reference, force)]
+                ex.submit(build_oracle, force), ex.submit(build_reference, force, reference_root)]
         for f in futs:
             f.result()
     build_driver(force)
